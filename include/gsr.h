@@ -1,0 +1,157 @@
+/*
+ * gsr -- GB300-native 3D Gaussian Splatting forward rasterizer: C ABI.
+ *
+ * Plain pointers, sizes and a cudaStream_t; no framework types.  Every entry
+ * point is asynchronous on the given stream and returns GSR_OK,
+ * GSR_INVALID_ARG or GSR_CUDA_ERROR for launch-time problems.  Errors found on
+ * the device (key-buffer overflow, a bounded wait that expired) are recorded
+ * in the status word of the caller's workspace and are turned into a
+ * gsr_status by gsr_read_status().
+ *
+ * Each entry point replaces one launcher of the reference rasterizer
+ * (LuoLongZan/PolySplat, csrc/ops.h); the citation is given beside it.
+ * Device arrays use the reference layouts:
+ *   pos [P,3] f32, shs [P,48] f32 or f16 (interleaved [P,16,3]),
+ *   opacity [P] f32, cov3d [P,6] f32 (xx,xy,xz,yy,yz,zz),
+ *   points_xy [P,2] f32, rgb_depth [P,4] f32, conic_opacity [P,4] f32,
+ *   keys u64 = tile << 32 | float_bits(view depth), values u32 = Gaussian index,
+ *   ranges int32 [tiles,2], image uint8 [H,W,3].
+ * Camera position (3 floats) and rotation (3x3 row-major camera-to-world, as
+ * in cameras.json) and the background colour are HOST pointers, read on the
+ * host exactly as the reference's bindings do (csrc/pybind.cpp:131-143).
+ */
+#ifndef GSR_H_
+#define GSR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* gsr_stream_t; /* == cudaStream_t */
+
+typedef enum {
+    GSR_OK = 0,
+    GSR_OVERFLOW = 1,      /* more keys than the key buffer holds; true count reported */
+    GSR_TIMEOUT = 2,       /* a bounded device-side wait expired */
+    GSR_INVALID_ARG = 3,
+    GSR_CUDA_ERROR = 4,
+} gsr_status;
+
+/* Render variants: the blend of every variant name the reference exposes
+ * maps onto one of these (tile size, exit-check cadence, range source). */
+typedef enum {
+    GSR_RENDER_PERSISTENT_RANGES = 0, /* render_16x16_preranges_smem_persistent_lite (render.cu:1717-1864): cadence 8 */
+    GSR_RENDER_PERSISTENT_FUSED = 1,  /* ..._lite_fused (render.cu:2026-2174): ranges found in-kernel, cadence 16 */
+    GSR_RENDER_DEFAULT = 2,           /* render_16x16 / renderCUDA (render.cu:2176): ranges in-kernel, cadence 2 */
+    GSR_RENDER_RANGES_CADENCE2 = 3,   /* preranges variants with per-pair exit checks */
+    GSR_RENDER_DT = 4,                /* ..._lite_dt (render.cu:1871-2018): skips power < log2(1/255), cadence 8 */
+} gsr_render_variant;
+
+/* Library version and a check that a CUDA device of compute capability 10.3
+ * is present (returns GSR_CUDA_ERROR otherwise). */
+int gsr_version(void);
+gsr_status gsr_device_check(int device);
+
+/* ---- workspace ---------------------------------------------------------- */
+/* Bytes of device workspace for a frame whose key buffer holds `capacity`
+ * keys: radix-sort ping-pong buffers and look-back state, the tile-queue
+ * counter and the status word.  Replaces get_sort_buffer_size
+ * (csrc/cuda_rasterizer/sort.cu:127-149, csrc/pybind.cpp:346-349); the
+ * workspace is the reference's `list_sorting_space`. */
+size_t gsr_workspace_size(int64_t capacity);
+/* Small workspace (status word + tile queue) for render-only calls. */
+size_t gsr_render_workspace_size(void);
+/* Clear the workspace's status word (asynchronous). */
+gsr_status gsr_workspace_reset(void* workspace, gsr_stream_t stream);
+/* Synchronise `stream`, read the status word and the key counter, and map
+ * them to a status.  *num_out receives the true key count (it may exceed
+ * capacity, in which case GSR_OVERFLOW is returned). */
+gsr_status gsr_read_status(const void* workspace, const int32_t* d_num, int64_t capacity, int32_t* num_out,
+                           gsr_stream_t stream);
+
+/* ---- scene preparation -------------------------------------------------- */
+/* Raw INRIA parameters -> render inputs: opacity = sigmoid(logit),
+ * cov3d = R S^2 R^T (upper triangle) with S = exp(log_scales) and R from the
+ * normalised w-first quaternion.  Replaces the CPU loop of loadPly_torch /
+ * computeCov3D (csrc/pybind.cpp:22-56, 105-117). */
+gsr_status gsr_scene_prepare(int P, const float* log_scales, const float* quats, const float* opacity_logits,
+                             float* opacity, float* cov3d, gsr_stream_t stream);
+
+/* ---- preprocess ---------------------------------------------------------- */
+/* Projection, EWA conic, degree-3 SH colour, culling and tile-key emission.
+ * Keys are appended at *curr_offset (atomically); writes past
+ * key_capacity are dropped but counted.  shs_half != 0 selects FP16 SH.
+ * Replaces preprocess / preprocess_half_sh (csrc/ops.h:42-48, 104-111;
+ * csrc/cuda_rasterizer/preprocess.cu:1252-1330; csrc/pybind.cpp:122-181). */
+gsr_status gsr_preprocess(int P, const float* pos, const void* shs, int shs_half, const float* opacity,
+                          const float* cov3d, int width, int height, int block_x, int block_y,
+                          const float* cam_pos, const float* cam_rot, float focal_x, float focal_y, float z_far,
+                          float z_near, float* points_xy, float* rgb_depth, float* conic_opacity, uint64_t* keys,
+                          uint32_t* values, int64_t key_capacity, int32_t* curr_offset, gsr_stream_t stream);
+
+/* ---- sort ----------------------------------------------------------------- */
+/* Stable ascending LSD radix sort of (u64 key, u32 value) pairs over bits
+ * [0, 32 + bits(tiles)).  The count is *d_num when d_num != NULL (device
+ * resident, no host sync), else num.  keys_in/values_in are preserved.
+ * Replaces sort_gaussian (csrc/cuda_rasterizer/sort.cu:107-125,
+ * csrc/pybind.cpp:333-344). */
+gsr_status gsr_sort(int num, const int32_t* d_num, int width, int height, int block_x, int block_y,
+                    void* workspace, size_t workspace_bytes, const uint64_t* keys_in, const uint32_t* values_in,
+                    uint64_t* keys_out, uint32_t* values_out, int64_t capacity, gsr_stream_t stream);
+
+/* Same sort over an explicit bit range [0, end_bit), end_bit in 1..64. */
+gsr_status gsr_sort_bits(int num, const int32_t* d_num, int end_bit, void* workspace, size_t workspace_bytes,
+                         const uint64_t* keys_in, const uint32_t* values_in, uint64_t* keys_out,
+                         uint32_t* values_out, int64_t capacity, gsr_stream_t stream);
+
+/* ---- tile ranges / gather ----------------------------------------------- */
+/* ranges[t] = [first, end) of tile t in the sorted keys.  scan_semantics = 0
+ * reproduces precompute_tile_ranges (binary search: empty tiles get
+ * start == end == lower bound; render.cu:10-35, 3510-3521, 6812-6824);
+ * scan_semantics = 1 reproduces precompute_tile_ranges_scan (empty tiles get
+ * {0,0}; render.cu:3526-3557, 6826-6845). */
+gsr_status gsr_tile_ranges(int num, const int32_t* d_num, int width, int height, int block_x, int block_y,
+                           const uint64_t* keys_sorted, int32_t* ranges, int scan_semantics, gsr_stream_t stream);
+
+/* dst[i] = src[values[i]] for xy, rgb_depth and conic_opacity.  Replaces
+ * gather_features (csrc/cuda_rasterizer/gather.cu:46-58, pybind.cpp:351-364). */
+gsr_status gsr_gather(int num, const int32_t* d_num, const uint32_t* values, const float* src_xy,
+                      const float* src_rgb_depth, const float* src_conic, float* dst_xy, float* dst_rgb_depth,
+                      float* dst_conic, gsr_stream_t stream);
+
+/* ---- render ------------------------------------------------------------- */
+/* Persistent tile-queue blend: one warp per tile, 32-Gaussian batches staged
+ * into shared memory by TMA bulk copies under mbarrier double-buffering,
+ * whole-tile early exit by warp vote, truncating uint8 encode.
+ * `ranges` is required for the *_RANGES/DT variants, `keys_sorted` for the
+ * FUSED/DEFAULT variants.  P is the length of the feature arrays (bounds).
+ * block_x/block_y select the tile shape (16x16, 24x16, 32x16, 32x32).
+ * Replaces render_16x16* / render_32x16* / render_32x32 / render_24x16_split
+ * (csrc/cuda_rasterizer/render.cu:4365-4385, 6445-6652; csrc/ops.h:164-354). */
+gsr_status gsr_render(int variant, int num, const int32_t* d_num, int width, int height, int block_x, int block_y,
+                      int P, const float* points_xy, const float* rgb_depth, const float* conic_opacity,
+                      const uint64_t* keys_sorted, const uint32_t* values_sorted, const int32_t* ranges,
+                      const float* bg_color, uint8_t* out_color, void* workspace, gsr_stream_t stream);
+
+/* ---- fused forward ------------------------------------------------------ */
+/* preprocess -> sort -> [ranges] -> render in one call, with the key count
+ * kept on the device (no host synchronisation; capturable in a CUDA graph).
+ * `ranges` may be NULL for the FUSED/DEFAULT variants.  Replaces
+ * forward_fused / forward_fused_e2e / forward_fused_e2e_preranges /
+ * sort_and_render (csrc/pybind.cpp:876-1149). */
+gsr_status gsr_forward(int variant, int P, const float* pos, const void* shs, int shs_half, const float* opacity,
+                       const float* cov3d, int width, int height, int block_x, int block_y, const float* cam_pos,
+                       const float* cam_rot, float focal_x, float focal_y, float z_far, float z_near,
+                       int32_t* curr_offset, void* workspace, size_t workspace_bytes, uint64_t* keys_unsorted,
+                       uint32_t* values_unsorted, uint64_t* keys_sorted, uint32_t* values_sorted,
+                       int64_t key_capacity, float* points_xy, float* rgb_depth, float* conic_opacity,
+                       int32_t* ranges, const float* bg_color, uint8_t* out_color, gsr_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSR_H_ */

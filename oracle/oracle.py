@@ -1,0 +1,187 @@
+"""ctypes front end of the FP64 CPU oracle (``gsr_oracle.c``) -- TEST INFRASTRUCTURE.
+
+Only the test suite, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU
+baseline leg use this module, and only as the checker; the product path
+(``polysplat_gb300``) never imports it.
+
+The C source restates the reference's equations in double precision; each
+function there cites the reference file:line it follows.  ``build()``
+compiles it with the host ``gcc`` into ``oracle/_build/``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libgsr_oracle.so")
+SRC = os.path.join(HERE, "gsr_oracle.c")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(SRC):
+        tmp = LIB_PATH + ".tmp%d" % os.getpid()
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-o", tmp, SRC, "-lpthread", "-lm"])
+        os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        i32, i64, f32 = ctypes.c_int, ctypes.c_int64, ctypes.c_float
+        L.ora_scene_transform.argtypes = [i32, P, P, P, P, P]
+        L.ora_scene_transform.restype = None
+        L.ora_preprocess.argtypes = [i32, P, P, P, P, i32, i32, i32, i32, P, P, f32, f32, f32, f32,
+                                     P, P, P, P, P, P, i64, i32]
+        L.ora_preprocess.restype = i64
+        L.ora_higher_msb.argtypes = [ctypes.c_uint32]
+        L.ora_higher_msb.restype = ctypes.c_uint32
+        L.ora_sort_pairs.argtypes = [i64, P, P, P, P, i32]
+        L.ora_sort_pairs.restype = None
+        L.ora_tile_ranges_bsearch.argtypes = [i64, P, i32, P]
+        L.ora_tile_ranges_bsearch.restype = None
+        L.ora_tile_ranges_scan.argtypes = [i64, P, i32, P]
+        L.ora_tile_ranges_scan.restype = None
+        L.ora_gather.argtypes = [i64, P, P, P, P, P, P, P]
+        L.ora_gather.restype = None
+        L.ora_render.argtypes = [i64, P, P, P, P, P, i32, i32, i32, i32, i32, i32, P, P, P, i32]
+        L.ora_render.restype = None
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"], "oracle arrays must be contiguous"
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def nthreads_default() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+def scene_transform(log_scales, quats, logits):
+    """Raw parameters -> (opacity [P], cov3d [P,6]) (``csrc/pybind.cpp:22-56,105-117``)."""
+    ls, q, lg = _c(log_scales, np.float32), _c(quats, np.float32), _c(logits, np.float32)
+    n = lg.shape[0]
+    op = np.empty(n, np.float32)
+    cov = np.empty((n, 6), np.float32)
+    lib().ora_scene_transform(n, _p(ls), _p(q), _p(lg), _p(op), _p(cov))
+    return op, cov
+
+
+def camera_args(cam):
+    return (_c(cam.position, np.float32).reshape(3), _c(cam.rotation, np.float32).reshape(9))
+
+
+def preprocess(pos, shs, opacity, cov3d, W, H, cam_pos, cam_rot, fx, fy, bx=16, by=16,
+               zfar=100.0, znear=0.01, capacity=None, nthreads=None):
+    """Returns dict(num, keys, vals, xy, rgbd, con, emitted)."""
+    pos, shs = _c(pos, np.float32), _c(shs, np.float32).reshape(-1, 48)
+    op, cov = _c(opacity, np.float32), _c(cov3d, np.float32)
+    P = op.shape[0]
+    cp, cr = _c(cam_pos, np.float32).reshape(3), _c(cam_rot, np.float32).reshape(9)
+    xy = np.zeros((P, 2), np.float32)
+    rgbd = np.zeros((P, 4), np.float32)
+    con = np.zeros((P, 4), np.float32)
+    emitted = np.zeros(P, np.uint8)
+    nt = nthreads or nthreads_default()
+    if capacity is None:
+        m = lib().ora_preprocess(P, _p(pos), _p(shs), _p(op), _p(cov), W, H, bx, by, _p(cp), _p(cr),
+                                 fx, fy, zfar, znear, _p(xy), _p(rgbd), _p(con), _p(emitted),
+                                 None, None, 0, nt)
+        capacity = m
+    keys = np.zeros(max(capacity, 1), np.uint64)
+    vals = np.zeros(max(capacity, 1), np.uint32)
+    m = lib().ora_preprocess(P, _p(pos), _p(shs), _p(op), _p(cov), W, H, bx, by, _p(cp), _p(cr),
+                             fx, fy, zfar, znear, _p(xy), _p(rgbd), _p(con), _p(emitted),
+                             _p(keys), _p(vals), capacity, nt)
+    k = min(m, capacity)
+    return dict(num=int(m), keys=keys[:k], vals=vals[:k], xy=xy, rgbd=rgbd, con=con,
+                emitted=emitted.astype(bool))
+
+
+def higher_msb(n: int) -> int:
+    return int(lib().ora_higher_msb(n))
+
+
+def end_bit_for(W, H, bx=16, by=16) -> int:
+    gx, gy = (W + bx - 1) // bx, (H + by - 1) // by
+    return 32 + higher_msb(gx * gy)
+
+
+def sort_pairs(keys, vals, end_bit=64):
+    k, v = _c(keys, np.uint64), _c(vals, np.uint32)
+    n = k.shape[0]
+    ko = np.empty_like(k)
+    vo = np.empty_like(v)
+    lib().ora_sort_pairs(n, _p(k), _p(v), _p(ko), _p(vo), end_bit)
+    return ko, vo
+
+
+def tile_ranges(keys, tiles, scan=False):
+    k = _c(keys, np.uint64)
+    r = np.empty((tiles, 2), np.int32)
+    fn = lib().ora_tile_ranges_scan if scan else lib().ora_tile_ranges_bsearch
+    fn(k.shape[0], _p(k), tiles, _p(r))
+    return r
+
+
+def gather(vals, xy, rgbd, con):
+    v = _c(vals, np.uint32)
+    xy, rgbd, con = _c(xy, np.float32), _c(rgbd, np.float32), _c(con, np.float32)
+    n = v.shape[0]
+    dxy = np.empty((n, 2), np.float32)
+    drgbd = np.empty((n, 4), np.float32)
+    dcon = np.empty((n, 4), np.float32)
+    lib().ora_gather(n, _p(v), _p(xy), _p(rgbd), _p(con), _p(dxy), _p(drgbd), _p(dcon))
+    return dxy, drgbd, dcon
+
+
+def render(vals, ranges, xy, rgbd, con, W, H, bg=(0.0, 0.0, 0.0), bx=16, by=16, cadence=8,
+           dt=False, nthreads=None, want_counts=False):
+    v, r = _c(vals, np.uint32), _c(ranges, np.int32)
+    xy, rgbd, con = _c(xy, np.float32), _c(rgbd, np.float32), _c(con, np.float32)
+    bgc = _c(bg, np.float32).reshape(3)
+    out = np.zeros((H, W, 3), np.uint8)
+    tiles = ((W + bx - 1) // bx) * ((H + by - 1) // by)
+    counts = np.zeros(tiles, np.int64) if want_counts else None
+    lib().ora_render(v.shape[0], _p(v), _p(r), _p(xy), _p(rgbd), _p(con), W, H, bx, by, cadence,
+                     1 if dt else 0, _p(bgc), _p(out), _p(counts) if counts is not None else None,
+                     nthreads or nthreads_default())
+    return (out, counts) if want_counts else out
+
+
+def forward(pos, shs, opacity, cov3d, cam, bg=(0.0, 0.0, 0.0), bx=16, by=16, cadence=8,
+            half_sh=False, nthreads=None):
+    """Whole forward: preprocess -> sort -> ranges -> blend.  Returns (image, dict)."""
+    shs = _c(shs, np.float32).reshape(-1, 48)
+    if half_sh:
+        shs = shs.astype(np.float16).astype(np.float32)
+    cp, cr = camera_args(cam)
+    pre = preprocess(pos, shs, opacity, cov3d, cam.width, cam.height, cp, cr, cam.fx, cam.fy,
+                     bx, by, nthreads=nthreads)
+    eb = end_bit_for(cam.width, cam.height, bx, by)
+    ks, vs = sort_pairs(pre["keys"], pre["vals"], eb)
+    tiles = ((cam.width + bx - 1) // bx) * ((cam.height + by - 1) // by)
+    rng = tile_ranges(ks, tiles)
+    img = render(vs, rng, pre["xy"], pre["rgbd"], pre["con"], cam.width, cam.height, bg, bx, by,
+                 cadence, nthreads=nthreads)
+    pre.update(keys_sorted=ks, vals_sorted=vs, ranges=rng, end_bit=eb)
+    return img, pre

@@ -1,0 +1,80 @@
+"""ctypes binding of ``libgsr.so`` (the C ABI declared in ``include/gsr.h``).
+
+The library is built in-tree by :mod:`polysplat_gb300.build`.  There is no
+fallback: if the shared library is missing or no GB300 is present, every
+entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+GSR_OK, GSR_OVERFLOW, GSR_TIMEOUT, GSR_INVALID_ARG, GSR_CUDA_ERROR = range(5)
+STATUS_NAMES = {0: "OK", 1: "OVERFLOW", 2: "TIMEOUT", 3: "INVALID_ARG", 4: "CUDA_ERROR"}
+
+RENDER_PERSISTENT_RANGES = 0
+RENDER_PERSISTENT_FUSED = 1
+RENDER_DEFAULT = 2
+RENDER_RANGES_CADENCE2 = 3
+RENDER_DT = 4
+
+
+class GsrError(RuntimeError):
+    def __init__(self, status: int, where: str, num: int = -1):
+        self.status = status
+        self.num = num
+        msg = "gsr %s failed: %s" % (where, STATUS_NAMES.get(status, str(status)))
+        if status == GSR_OVERFLOW:
+            msg += " (%d keys emitted; the key buffers are too small)" % num
+        super().__init__(msg)
+
+
+def _declare(L):
+    P, i32, i64, f32, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_size_t
+    sig = {
+        "gsr_version": ([], i32),
+        "gsr_device_check": ([i32], i32),
+        "gsr_workspace_size": ([i64], sz),
+        "gsr_render_workspace_size": ([], sz),
+        "gsr_workspace_reset": ([P, P], i32),
+        "gsr_read_status": ([P, P, i64, P, P], i32),
+        "gsr_scene_prepare": ([i32, P, P, P, P, P, P], i32),
+        "gsr_preprocess": ([i32, P, P, i32, P, P, i32, i32, i32, i32, P, P, f32, f32, f32, f32,
+                            P, P, P, P, P, i64, P, P], i32),
+        "gsr_sort": ([i32, P, i32, i32, i32, i32, P, sz, P, P, P, P, i64, P], i32),
+        "gsr_sort_bits": ([i32, P, i32, P, sz, P, P, P, P, i64, P], i32),
+        "gsr_tile_ranges": ([i32, P, i32, i32, i32, i32, P, P, i32, P], i32),
+        "gsr_gather": ([i32, P, P, P, P, P, P, P, P, P], i32),
+        "gsr_render": ([i32, i32, P, i32, i32, i32, i32, i32, P, P, P, P, P, P, P, P, P, P], i32),
+        "gsr_forward": ([i32, i32, P, P, i32, P, P, i32, i32, i32, i32, P, P, f32, f32, f32, f32,
+                         P, P, sz, P, P, P, P, i64, P, P, P, P, P, P, P], i32),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    return L
+
+
+def lib():
+    """Load (building first if needed) the gsr shared library."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                path = _build.LIB
+                if not os.path.exists(path) or os.environ.get("GSR_REBUILD"):
+                    path = _build.build()
+                _lib = _declare(ctypes.CDLL(path))
+    return _lib
+
+
+def check(status: int, where: str, num: int = -1) -> None:
+    if status != GSR_OK:
+        raise GsrError(status, where, num)

@@ -1,0 +1,279 @@
+// C ABI of the gsr library (declared in include/gsr.h).
+#include <cstring>
+#include <mutex>
+
+#include "gsr_internal.h"
+
+namespace gsr {
+
+int device_sm_count()
+{
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    if (cached[dev] == 0) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        cached[dev] = n > 0 ? n : 1;
+    }
+    return cached[dev];
+}
+
+static gsr_status from_cuda(cudaError_t e)
+{
+    if (e == cudaSuccess) return GSR_OK;
+    if (e == cudaErrorInvalidValue) return GSR_INVALID_ARG;
+    return GSR_CUDA_ERROR;
+}
+
+static int tiles_of(int W, int H, int bx, int by) { return div_up(W, bx) * div_up(H, by); }
+
+static bool render_needs_ranges(int variant)
+{
+    return variant == GSR_RENDER_PERSISTENT_RANGES || variant == GSR_RENDER_RANGES_CADENCE2 ||
+           variant == GSR_RENDER_DT;
+}
+
+static bool valid_tile_shape(int bx, int by)
+{
+    return (bx == 16 && by == 16) || (bx == 32 && by == 16) || (bx == 24 && by == 16) || (bx == 32 && by == 32);
+}
+
+}  // namespace gsr
+
+using namespace gsr;
+
+extern "C" {
+
+int gsr_version(void) { return 1; }
+
+gsr_status gsr_device_check(int device)
+{
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return GSR_CUDA_ERROR;
+    if (prop.major != 10 || prop.minor != 3) return GSR_CUDA_ERROR;
+    return GSR_OK;
+}
+
+size_t gsr_workspace_size(int64_t capacity) { return sort_workspace_bytes(capacity); }
+
+size_t gsr_render_workspace_size(void) { return kHeaderBytes; }
+
+gsr_status gsr_workspace_reset(void* workspace, gsr_stream_t stream)
+{
+    if (!workspace) return GSR_INVALID_ARG;
+    return from_cuda(cudaMemsetAsync(workspace, 0, sizeof(uint32_t), (cudaStream_t)stream));
+}
+
+gsr_status gsr_read_status(const void* workspace, const int32_t* d_num, int64_t capacity, int32_t* num_out,
+                           gsr_stream_t stream)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return GSR_CUDA_ERROR;
+    uint32_t status = 0;
+    int32_t num = 0;
+    if (workspace && cudaMemcpy(&status, workspace, sizeof(uint32_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return GSR_CUDA_ERROR;
+    if (d_num && cudaMemcpy(&num, d_num, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return GSR_CUDA_ERROR;
+    if (num_out) *num_out = num;
+    if (status & kErrTimeout) return GSR_TIMEOUT;
+    if (d_num && (int64_t)num > capacity) return GSR_OVERFLOW;
+    if (status & kErrOverflow) return GSR_OVERFLOW;
+    if (status & kErrBadInput) return GSR_INVALID_ARG;
+    return GSR_OK;
+}
+
+gsr_status gsr_scene_prepare(int P, const float* log_scales, const float* quats, const float* opacity_logits,
+                             float* opacity, float* cov3d, gsr_stream_t stream)
+{
+    if (P < 0 || (P > 0 && (!log_scales || !quats || !opacity_logits || !opacity || !cov3d))) return GSR_INVALID_ARG;
+    return from_cuda(launch_scene_prepare(P, log_scales, quats, opacity_logits, opacity, cov3d, (cudaStream_t)stream));
+}
+
+static gsr_status preprocess_impl(int P, const float* pos, const void* shs, int shs_half, const float* opacity,
+                                  const float* cov3d, int width, int height, int block_x, int block_y,
+                                  const float* cam_pos, const float* cam_rot, float fx, float fy, float zfar,
+                                  float znear, float* points_xy, float* rgb_depth, float* conic_opacity,
+                                  uint64_t* keys, uint32_t* values, int64_t cap, int32_t* curr_offset,
+                                  cudaStream_t s)
+{
+    if (P < 0 || width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0 || !cam_pos || !cam_rot || !curr_offset)
+        return GSR_INVALID_ARG;
+    if (P > 0 && (!pos || !shs || !opacity || !cov3d || !points_xy || !rgb_depth || !conic_opacity))
+        return GSR_INVALID_ARG;
+    if (cap > 0 && (!keys || !values)) return GSR_INVALID_ARG;
+    PreprocessParams p;
+    p.P = P;
+    p.pos = pos;
+    p.shs = shs;
+    p.opacity = opacity;
+    p.cov3d = cov3d;
+    p.W = width;
+    p.H = height;
+    p.bx = block_x;
+    p.by = block_y;
+    p.gx = div_up(width, block_x);
+    p.gy = div_up(height, block_y);
+    camera_matrices(width, height, cam_pos, cam_rot, fx, fy, zfar, znear, p.view, p.proj);
+    p.campos[0] = cam_pos[0];
+    p.campos[1] = cam_pos[1];
+    p.campos[2] = cam_pos[2];
+    p.tanx = width / (2.0f * fx);
+    p.tany = height / (2.0f * fy);
+    p.fx = fx;
+    p.fy = fy;
+    p.points_xy = reinterpret_cast<float2*>(points_xy);
+    p.rgb_depth = reinterpret_cast<float4*>(rgb_depth);
+    p.conic_opacity = reinterpret_cast<float4*>(conic_opacity);
+    p.keys = keys;
+    p.vals = values;
+    p.cap = cap;
+    p.counter = curr_offset;
+    return from_cuda(launch_preprocess(p, shs_half != 0, s));
+}
+
+gsr_status gsr_preprocess(int P, const float* pos, const void* shs, int shs_half, const float* opacity,
+                          const float* cov3d, int width, int height, int block_x, int block_y, const float* cam_pos,
+                          const float* cam_rot, float focal_x, float focal_y, float z_far, float z_near,
+                          float* points_xy, float* rgb_depth, float* conic_opacity, uint64_t* keys, uint32_t* values,
+                          int64_t key_capacity, int32_t* curr_offset, gsr_stream_t stream)
+{
+    return preprocess_impl(P, pos, shs, shs_half, opacity, cov3d, width, height, block_x, block_y, cam_pos, cam_rot,
+                           focal_x, focal_y, z_far, z_near, points_xy, rgb_depth, conic_opacity, keys, values,
+                           key_capacity, curr_offset, (cudaStream_t)stream);
+}
+
+gsr_status gsr_sort_bits(int num, const int32_t* d_num, int end_bit, void* workspace, size_t workspace_bytes,
+                         const uint64_t* keys_in, const uint32_t* values_in, uint64_t* keys_out, uint32_t* values_out,
+                         int64_t capacity, gsr_stream_t stream)
+{
+    if (!workspace || end_bit < 1 || end_bit > 64 || capacity < 0 || (!d_num && num < 0)) return GSR_INVALID_ARG;
+    if (!d_num && num > capacity) return GSR_INVALID_ARG;
+    if (capacity > 0 && (!keys_in || !values_in || !keys_out || !values_out)) return GSR_INVALID_ARG;
+    if (keys_in == keys_out || values_in == values_out) return GSR_INVALID_ARG;
+    SortArgs a;
+    a.num = num;
+    a.d_num = d_num;
+    a.cap = capacity;
+    a.end_bit = end_bit;
+    a.keys_in = keys_in;
+    a.vals_in = values_in;
+    a.keys_out = keys_out;
+    a.vals_out = values_out;
+    a.ws = workspace;
+    a.ws_bytes = workspace_bytes;
+    return from_cuda(launch_sort(a, (cudaStream_t)stream));
+}
+
+gsr_status gsr_sort(int num, const int32_t* d_num, int width, int height, int block_x, int block_y, void* workspace,
+                    size_t workspace_bytes, const uint64_t* keys_in, const uint32_t* values_in, uint64_t* keys_out,
+                    uint32_t* values_out, int64_t capacity, gsr_stream_t stream)
+{
+    if (width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0) return GSR_INVALID_ARG;
+    const int end_bit = 32 + bits_for((uint32_t)tiles_of(width, height, block_x, block_y));
+    return gsr_sort_bits(num, d_num, end_bit, workspace, workspace_bytes, keys_in, values_in, keys_out, values_out,
+                         capacity, stream);
+}
+
+gsr_status gsr_tile_ranges(int num, const int32_t* d_num, int width, int height, int block_x, int block_y,
+                           const uint64_t* keys_sorted, int32_t* ranges, int scan_semantics, gsr_stream_t stream)
+{
+    if (width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0 || !ranges || (!d_num && num < 0))
+        return GSR_INVALID_ARG;
+    const long long cap = d_num ? (long long)INT32_MAX : (long long)num;
+    return from_cuda(launch_tile_ranges(num, d_num, cap, tiles_of(width, height, block_x, block_y), keys_sorted,
+                                        ranges, scan_semantics != 0, (cudaStream_t)stream));
+}
+
+gsr_status gsr_gather(int num, const int32_t* d_num, const uint32_t* values, const float* src_xy,
+                      const float* src_rgb_depth, const float* src_conic, float* dst_xy, float* dst_rgb_depth,
+                      float* dst_conic, gsr_stream_t stream)
+{
+    if (!d_num && num < 0) return GSR_INVALID_ARG;
+    if (d_num) return GSR_INVALID_ARG;  // the destination size must be known: pass the host count
+    return from_cuda(launch_gather(num, nullptr, values, reinterpret_cast<const float2*>(src_xy),
+                                   reinterpret_cast<const float4*>(src_rgb_depth),
+                                   reinterpret_cast<const float4*>(src_conic), reinterpret_cast<float2*>(dst_xy),
+                                   reinterpret_cast<float4*>(dst_rgb_depth), reinterpret_cast<float4*>(dst_conic),
+                                   (long long)num, (cudaStream_t)stream));
+}
+
+static gsr_status render_impl(int variant, int num, const int32_t* d_num, long long cap, int width, int height,
+                              int block_x, int block_y, int P, const float* points_xy, const float* rgb_depth,
+                              const float* conic_opacity, const uint64_t* keys_sorted, const uint32_t* values_sorted,
+                              const int32_t* ranges, const float* bg_color, uint8_t* out_color, void* workspace,
+                              cudaStream_t s)
+{
+    if (!workspace || !out_color || !bg_color || width <= 0 || height <= 0 || !valid_tile_shape(block_x, block_y))
+        return GSR_INVALID_ARG;
+    if (render_needs_ranges(variant) ? !ranges : !keys_sorted) return GSR_INVALID_ARG;
+    if (variant < 0 || variant > GSR_RENDER_DT) return GSR_INVALID_ARG;
+    RenderArgs a;
+    a.variant = variant;
+    a.num = num;
+    a.d_num = d_num;
+    a.cap = cap;
+    a.W = width;
+    a.H = height;
+    a.bx = block_x;
+    a.by = block_y;
+    a.P = P;
+    a.xy = reinterpret_cast<const float2*>(points_xy);
+    a.rgbd = reinterpret_cast<const float4*>(rgb_depth);
+    a.con = reinterpret_cast<const float4*>(conic_opacity);
+    a.keys = keys_sorted;
+    a.vals = values_sorted;
+    a.ranges = reinterpret_cast<const int2*>(ranges);
+    a.bg[0] = bg_color[0];
+    a.bg[1] = bg_color[1];
+    a.bg[2] = bg_color[2];
+    a.out = out_color;
+    a.ws = reinterpret_cast<WorkspaceHeader*>(workspace);
+    return from_cuda(launch_render(a, s));
+}
+
+gsr_status gsr_render(int variant, int num, const int32_t* d_num, int width, int height, int block_x, int block_y,
+                      int P, const float* points_xy, const float* rgb_depth, const float* conic_opacity,
+                      const uint64_t* keys_sorted, const uint32_t* values_sorted, const int32_t* ranges,
+                      const float* bg_color, uint8_t* out_color, void* workspace, gsr_stream_t stream)
+{
+    if (!d_num && num < 0) return GSR_INVALID_ARG;
+    return render_impl(variant, num, d_num, d_num ? (long long)INT32_MAX : (long long)num, width, height, block_x,
+                       block_y, P, points_xy, rgb_depth, conic_opacity, keys_sorted, values_sorted, ranges, bg_color,
+                       out_color, workspace, (cudaStream_t)stream);
+}
+
+gsr_status gsr_forward(int variant, int P, const float* pos, const void* shs, int shs_half, const float* opacity,
+                       const float* cov3d, int width, int height, int block_x, int block_y, const float* cam_pos,
+                       const float* cam_rot, float focal_x, float focal_y, float z_far, float z_near,
+                       int32_t* curr_offset, void* workspace, size_t workspace_bytes, uint64_t* keys_unsorted,
+                       uint32_t* values_unsorted, uint64_t* keys_sorted, uint32_t* values_sorted,
+                       int64_t key_capacity, float* points_xy, float* rgb_depth, float* conic_opacity,
+                       int32_t* ranges, const float* bg_color, uint8_t* out_color, gsr_stream_t stream)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!workspace || !curr_offset || !valid_tile_shape(block_x, block_y)) return GSR_INVALID_ARG;
+    if (render_needs_ranges(variant) && !ranges) return GSR_INVALID_ARG;
+    if (workspace_bytes < sort_workspace_bytes(key_capacity)) return GSR_INVALID_ARG;
+    cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(uint32_t), s);  // status word
+    if (e == cudaSuccess) e = cudaMemsetAsync(curr_offset, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess) return from_cuda(e);
+    gsr_status st = preprocess_impl(P, pos, shs, shs_half, opacity, cov3d, width, height, block_x, block_y, cam_pos,
+                                    cam_rot, focal_x, focal_y, z_far, z_near, points_xy, rgb_depth, conic_opacity,
+                                    keys_unsorted, values_unsorted, key_capacity, curr_offset, s);
+    if (st != GSR_OK) return st;
+    const int tiles = tiles_of(width, height, block_x, block_y);
+    st = gsr_sort_bits(0, curr_offset, 32 + bits_for((uint32_t)tiles), workspace, workspace_bytes, keys_unsorted,
+                       values_unsorted, keys_sorted, values_sorted, key_capacity, stream);
+    if (st != GSR_OK) return st;
+    if (render_needs_ranges(variant)) {
+        e = launch_tile_ranges(0, curr_offset, key_capacity, tiles, keys_sorted, ranges, false, s);
+        if (e != cudaSuccess) return from_cuda(e);
+    }
+    return render_impl(variant, 0, curr_offset, key_capacity, width, height, block_x, block_y, P, points_xy,
+                       rgb_depth, conic_opacity, keys_sorted, values_sorted, ranges, bg_color, out_color, workspace,
+                       s);
+}
+
+}  // extern "C"

@@ -1,0 +1,96 @@
+// Internal launch interfaces shared between the gsr translation units.
+#pragma once
+
+#include "gsr_common.cuh"
+
+namespace gsr {
+
+struct PreprocessParams {
+    int P;
+    const float* pos;
+    const void* shs;
+    const float* opacity;
+    const float* cov3d;
+    int W, H, bx, by, gx, gy;
+    float view[16];  // column-major
+    float proj[16];  // column-major
+    float campos[3];
+    float tanx, tany, fx, fy;
+    float2* points_xy;
+    float4* rgb_depth;
+    float4* conic_opacity;
+    uint64_t* keys;
+    uint32_t* vals;
+    long long cap;
+    int* counter;
+};
+
+void camera_matrices(int W, int H, const float* pos, const float* rot, float fx, float fy, float zfar, float znear,
+                     float* view, float* proj);
+cudaError_t launch_preprocess(const PreprocessParams& p, bool half_sh, cudaStream_t stream);
+cudaError_t launch_scene_prepare(int P, const float* log_scales, const float* quats, const float* logits,
+                                 float* opacity, float* cov3d, cudaStream_t stream);
+
+// ---- workspace layout ----------------------------------------------------
+// [0, kHeaderBytes): header (status word, counters, histograms)
+// then: sort alternate keys (8*cap), alternate values (4*cap), look-back
+// state (passes * tiles * 256 * 4).
+struct WorkspaceHeader {
+    uint32_t status;          // OR of kErr* bits
+    uint32_t render_queue;    // persistent render tile counter
+    uint32_t pass_counter[8]; // per radix pass tile counter
+    uint32_t pad[6];
+    uint32_t hist[8][256];    // per-pass digit histograms
+};
+constexpr size_t kHeaderBytes = 16384;
+static_assert(sizeof(WorkspaceHeader) <= kHeaderBytes, "header too large");
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per tile
+constexpr int kMaxPasses = 8;
+
+size_t sort_workspace_bytes(long long cap);
+
+struct SortArgs {
+    int num;                // host count (used when d_num == nullptr)
+    const int32_t* d_num;   // device count or nullptr
+    long long cap;          // capacity of the key buffers
+    int end_bit;
+    const uint64_t* keys_in;
+    const uint32_t* vals_in;
+    uint64_t* keys_out;
+    uint32_t* vals_out;
+    void* ws;
+    size_t ws_bytes;
+};
+cudaError_t launch_sort(const SortArgs& a, cudaStream_t stream);
+
+cudaError_t launch_tile_ranges(int num, const int32_t* d_num, long long cap, int tiles, const uint64_t* keys,
+                               int32_t* ranges, bool scan_semantics, cudaStream_t stream);
+cudaError_t launch_gather(int num, const int32_t* d_num, const uint32_t* values, const float2* sxy,
+                          const float4* srgbd, const float4* scon, float2* dxy, float4* drgbd, float4* dcon,
+                          long long cap, cudaStream_t stream);
+
+struct RenderArgs {
+    int variant;
+    int num;
+    const int32_t* d_num;
+    long long cap;  // key-buffer capacity: the device count is clamped to it
+    int W, H, bx, by;
+    int P;
+    const float2* xy;
+    const float4* rgbd;
+    const float4* con;
+    const uint64_t* keys;
+    const uint32_t* vals;
+    const int2* ranges;
+    float bg[3];
+    uint8_t* out;
+    WorkspaceHeader* ws;
+};
+cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream);
+
+int device_sm_count();
+
+}  // namespace gsr

@@ -1,0 +1,567 @@
+// Scene preparation and preprocess (projection, EWA conic, SH colour, culling,
+// tile-key emission) for sm_103a.
+//
+// The arithmetic of the geometry, the SH colour and the tile tests follows
+// the reference's expressions operation for operation
+// (csrc/cuda_rasterizer/preprocess.cu:78-311, 354-413) and is compiled with
+// the same fast-math flags, so that the emitted (tile, depth) keys agree
+// with the reference build bit for bit.  The kernel structure is this
+// library's own: 8 warps per CTA, each warp owns 32 consecutive Gaussians,
+// and keys are staged per warp in shared memory and flushed with one global
+// atomic per flush instead of one per 32-wide emission step.
+#include "gsr_internal.h"
+
+namespace gsr {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Tiny vector / matrix types with the component semantics of the GLM calls in
+// the reference (column-major mat3, left-to-right sums of products).
+
+struct V3 {
+    float x, y, z;
+    // member form so that it also applies to temporaries, as glm's does
+    __device__ __forceinline__ V3& operator+=(float s)
+    {
+        x += s;
+        y += s;
+        z += s;
+        return *this;
+    }
+};
+__device__ __forceinline__ V3 operator*(float s, V3 v) { return {s * v.x, s * v.y, s * v.z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+
+struct M3 {
+    float m[3][3];  // m[column][row]
+};
+
+__device__ __forceinline__ M3 m3_mul(const M3& a, const M3& b)
+{
+    M3 r;
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) r.m[c][k] = a.m[0][k] * b.m[c][0] + a.m[1][k] * b.m[c][1] + a.m[2][k] * b.m[c][2];
+    return r;
+}
+
+__device__ __forceinline__ M3 m3_transpose(const M3& a)
+{
+    M3 r;
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) r.m[c][k] = a.m[k][c];
+    return r;
+}
+
+__device__ __forceinline__ M3 m3_cols(float a0, float a1, float a2, float b0, float b1, float b2, float c0, float c1,
+                                      float c2)
+{
+    M3 r;
+    r.m[0][0] = a0; r.m[0][1] = a1; r.m[0][2] = a2;
+    r.m[1][0] = b0; r.m[1][1] = b1; r.m[1][2] = b2;
+    r.m[2][0] = c0; r.m[2][1] = c1; r.m[2][2] = c2;
+    return r;
+}
+
+// Constants of preprocess.cu:13-38.
+constexpr float kLog2e = 1.4426950216293334961f;
+constexpr float kLn2 = 0.69314718055f;
+constexpr float kCutoff = 8.0f;
+constexpr float kBMinSq = 0.09f;
+constexpr float kOThin = 0.5f;
+#define GSR_SH_C0 0.28209479177387814f
+#define GSR_SH_C1 0.4886025119029199f
+#define GSR_SH_C2_0 1.0925484305920792f
+#define GSR_SH_C2_1 (-1.0925484305920792f)
+#define GSR_SH_C2_2 0.31539156525252005f
+#define GSR_SH_C2_3 (-1.0925484305920792f)
+#define GSR_SH_C2_4 0.5462742152960396f
+#define GSR_SH_C3_0 (-0.5900435899266435f)
+#define GSR_SH_C3_1 2.890611442640554f
+#define GSR_SH_C3_2 (-0.4570457994644658f)
+#define GSR_SH_C3_3 0.3731763325901154f
+#define GSR_SH_C3_4 (-0.4570457994644658f)
+#define GSR_SH_C3_5 1.445305721320277f
+#define GSR_SH_C3_6 (-0.5900435899266435f)
+
+__device__ __forceinline__ float ndc_to_pix(float v, int S) { return ((v + 1.0) * S - 1.0) * 0.5; }
+
+__device__ __forceinline__ float3 xform43(V3 p, const float* m)
+{
+    return {m[0] * p.x + m[4] * p.y + m[8] * p.z + m[12], m[1] * p.x + m[5] * p.y + m[9] * p.z + m[13],
+            m[2] * p.x + m[6] * p.y + m[10] * p.z + m[14]};
+}
+
+__device__ __forceinline__ float4 xform44(V3 p, const float* m)
+{
+    return {m[0] * p.x + m[4] * p.y + m[8] * p.z + m[12], m[1] * p.x + m[5] * p.y + m[9] * p.z + m[13],
+            m[2] * p.x + m[6] * p.y + m[10] * p.z + m[14], m[3] * p.x + m[7] * p.y + m[11] * p.z + m[15]};
+}
+
+// EWA projection of the 3D covariance (Zwicker et al. 2002, eqs. 29/31) with
+// the 1.3*tan(fov) clamp and the +0.3 low-pass; same steps as
+// preprocess.cu:117-157.
+__device__ __forceinline__ float3 cov2d(V3 p, float fx, float fy, float tanx, float tany, const float* s,
+                                        const float* vm)
+{
+    float3 t = xform43(p, vm);
+    const float limx = 1.3f * tanx;
+    const float limy = 1.3f * tany;
+    const float txtz = t.x / t.z;
+    const float tytz = t.y / t.z;
+    t.x = fminf(limx, fmaxf(-limx, txtz)) * t.z;
+    t.y = fminf(limy, fmaxf(-limy, tytz)) * t.z;
+    M3 J = m3_cols(fx / t.z, 0.0f, -(fx * t.x) / (t.z * t.z), 0.0f, fy / t.z, -(fy * t.y) / (t.z * t.z), 0, 0, 0);
+    M3 W = m3_cols(vm[0], vm[4], vm[8], vm[1], vm[5], vm[9], vm[2], vm[6], vm[10]);
+    M3 T = m3_mul(W, J);
+    M3 V = m3_cols(s[0], s[1], s[2], s[1], s[3], s[4], s[2], s[4], s[5]);
+    M3 cov = m3_mul(m3_mul(m3_transpose(T), m3_transpose(V)), T);
+    cov.m[0][0] += 0.3f;
+    cov.m[1][1] += 0.3f;
+    return {cov.m[0][0], cov.m[0][1], cov.m[1][1]};
+}
+
+// Degree-3 SH colour: +0.5 bias, clamp at 0 only (preprocess.cu:159-255).
+template <bool HALF>
+__device__ __forceinline__ V3 sh_color(int idx, V3 p, V3 cam, const void* shs)
+{
+    V3 dir = p - cam;
+    float l2 = dir.x * dir.x + dir.y * dir.y + dir.z * dir.z;
+    float r = rsqrt_approx(l2);
+    dir.x *= r;
+    dir.y *= r;
+    dir.z *= r;
+    V3 v[16];
+    if (HALF) {
+        const uint4* b4 = reinterpret_cast<const uint4*>(reinterpret_cast<const __half*>(shs) + (size_t)idx * 48);
+        uint4 raw[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) raw[k] = __ldg(b4 + k);
+        const __half* h = reinterpret_cast<const __half*>(raw);
+#pragma unroll
+        for (int k = 0; k < 16; k++) v[k] = {__half2float(h[3 * k]), __half2float(h[3 * k + 1]), __half2float(h[3 * k + 2])};
+    } else {
+        const float4* b4 = reinterpret_cast<const float4*>(reinterpret_cast<const float*>(shs) + (size_t)idx * 48);
+        float4 raw[12];
+#pragma unroll
+        for (int k = 0; k < 12; k++) raw[k] = __ldg(b4 + k);
+        const float* f = reinterpret_cast<const float*>(raw);
+#pragma unroll
+        for (int k = 0; k < 16; k++) v[k] = {f[3 * k], f[3 * k + 1], f[3 * k + 2]};
+    }
+    V3 result = GSR_SH_C0 * v[0] += 0.5f;
+    float x = dir.x, y = dir.y, z = dir.z;
+    result = result - GSR_SH_C1 * y * v[1] + GSR_SH_C1 * z * v[2] - GSR_SH_C1 * x * v[3];
+    float xx = x * x, yy = y * y, zz = z * z;
+    float xy = x * y, yz = y * z, xz = x * z;
+    result = result + GSR_SH_C2_0 * xy * v[4] + GSR_SH_C2_1 * yz * v[5] +
+             GSR_SH_C2_2 * (2.0f * zz - xx - yy) * v[6] + GSR_SH_C2_3 * xz * v[7] + GSR_SH_C2_4 * (xx - yy) * v[8];
+    result = result + GSR_SH_C3_0 * y * (3.0f * xx - yy) * v[9] + GSR_SH_C3_1 * xy * z * v[10] +
+             GSR_SH_C3_2 * y * (4.0f * zz - xx - yy) * v[11] +
+             GSR_SH_C3_3 * z * (2.0f * zz - 3.0f * xx - 3.0f * yy) * v[12] +
+             GSR_SH_C3_4 * x * (4.0f * zz - xx - yy) * v[13] + GSR_SH_C3_5 * z * (xx - yy) * v[14] +
+             GSR_SH_C3_6 * x * (xx - 3.0f * yy) * v[15];
+    result.x = fmaxf(result.x, 0.0f);
+    result.y = fmaxf(result.y, 0.0f);
+    result.z = fmaxf(result.z, 0.0f);
+    return result;
+}
+
+// Ellipse / tile-box tests (preprocess.cu:257-311).
+__device__ __forceinline__ bool seg_hits_ellipse(float a, float b, float c, float d, float l, float r)
+{
+    float delta = b * b - 4.0f * a * c;
+    float t1 = (l - d) * (2.0f * a) + b;
+    float t2 = (r - d) * (2.0f * a) + b;
+    return delta >= 0.0f && (t1 <= 0.0f || t1 * t1 <= delta) && (t2 >= 0.0f || t2 * t2 <= delta);
+}
+
+__device__ __forceinline__ bool box_hits_ellipse(int2 pmin, int2 pmax, float2 ctr, float3 con, float power)
+{
+    float a, b, c, dx, dy;
+    float w = 2.0f * power;
+    if (ctr.x * 2.0f < pmin.x + pmax.x) dx = ctr.x - pmin.x;
+    else dx = ctr.x - pmax.x;
+    a = con.z;
+    b = -2.0f * con.y * dx;
+    c = con.x * dx * dx - w;
+    if (seg_hits_ellipse(a, b, c, ctr.y, pmin.y, pmax.y)) return true;
+    if (ctr.y * 2.0f < pmin.y + pmax.y) dy = ctr.y - pmin.y;
+    else dy = ctr.y - pmax.y;
+    a = con.x;
+    b = -2.0f * con.y * dy;
+    c = con.z * dy * dy - w;
+    return seg_hits_ellipse(a, b, c, ctr.x, pmin.x, pmax.x);
+}
+
+__device__ __forceinline__ bool box_has_centre(int2 pmin, int2 pmax, float2 c)
+{
+    return c.x >= pmin.x && c.x <= pmax.x && c.y >= pmin.y && c.y <= pmax.y;
+}
+
+__device__ __forceinline__ bool tile_hit(int x, int y, int bx, int by, float2 ctr, float3 con, float power)
+{
+    int2 pmin = {x * bx, y * by};
+    int2 pmax = {pmin.x + bx - 1, pmin.y + by - 1};
+    return box_has_centre(pmin, pmax, ctr) || (power > 0.0f && box_hits_ellipse(pmin, pmax, ctr, con, power));
+}
+
+// ---------------------------------------------------------------------------
+// Per-warp key staging.  A warp appends up to 32 keys per step into its own
+// shared-memory ring; when the next step could overflow it, the warp
+// reserves space in the global key buffer with one atomicAdd and copies the
+// staged keys out with coalesced stores.
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+constexpr int kStage = 256;
+
+struct Stage {
+    uint64_t* k;
+    uint32_t* v;
+    int fill;
+};
+
+struct EmitOut {
+    uint64_t* keys;
+    uint32_t* vals;
+    long long cap;
+    int* counter;
+};
+
+__device__ __forceinline__ void stage_flush(Stage& s, const EmitOut& o, unsigned lane)
+{
+    __syncwarp();
+    int base = 0;
+    if (lane == 0) base = atomicAdd(o.counter, s.fill);
+    base = __shfl_sync(GSR_FULL_MASK, base, 0);
+    for (int i = lane; i < s.fill; i += 32) {
+        long long pos = (long long)base + i;
+        if (pos < o.cap) {
+            o.keys[pos] = s.k[i];
+            o.vals[pos] = s.v[i];
+        }
+    }
+    __syncwarp();
+    s.fill = 0;
+}
+
+__device__ __forceinline__ void stage_emit(Stage& s, const EmitOut& o, bool valid, uint64_t key, uint32_t val,
+                                           unsigned lane)
+{
+    unsigned mask = __ballot_sync(GSR_FULL_MASK, valid);
+    if (mask == 0) return;
+    int n = __popc(mask);
+    if (s.fill + n > kStage) stage_flush(s, o, lane);
+    if (valid) {
+        int slot = s.fill + __popc(mask & lanemask_lt());
+        s.k[slot] = key;
+        s.v[slot] = val;
+    }
+    s.fill += n;
+}
+
+__device__ __forceinline__ int warp_max(int v)
+{
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v = max(v, __shfl_xor_sync(GSR_FULL_MASK, v, d));
+    return v;
+}
+
+template <bool HALF>
+__global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessParams a)
+{
+    __shared__ uint64_t s_keys[kWarps][kStage];
+    __shared__ uint32_t s_vals[kWarps][kStage];
+    __shared__ int s_fill[kWarps];
+    __shared__ long long s_base[kWarps];
+    __shared__ uint32_t s_hit[kWarps];
+
+    const unsigned lane = threadIdx.x & 31u;
+    const int warp = threadIdx.x >> 5;
+    const int idx = blockIdx.x * kThreads + threadIdx.x;
+    const int warp_first = idx - (int)lane;
+    const int tx = lane & 7, ty = lane >> 3;  // 8x4 tile window of the massive path
+    const int gridx = a.gx, gridy = a.gy;
+
+    bool point_valid = false;
+    V3 p_orig = {0.f, 0.f, 0.f};
+    float3 p_view = {0.f, 0.f, 0.f};
+    float2 point_xy = {0.f, 0.f};
+    float3 conic = {0.f, 0.f, 0.f};
+    float opacity = 0.f, power = 0.f, log2_opacity = 0.f;
+    int width = 0, height = 0;
+    int2 rect_min = {0, 0}, rect_max = {0, 0};
+
+    if (idx < a.P) {
+        do {
+            p_orig = {__ldg(a.pos + 3 * (size_t)idx), __ldg(a.pos + 3 * (size_t)idx + 1),
+                      __ldg(a.pos + 3 * (size_t)idx + 2)};
+            p_view = xform43(p_orig, a.view);
+            if (p_view.z <= 0.2f) break;
+            opacity = __ldg(a.opacity + idx);
+            float4 p_hom = xform44(p_orig, a.proj);
+            float p_w = 1.0f / (p_hom.w + 0.0000001f);
+            float3 p_proj = {p_hom.x * p_w, p_hom.y * p_w, p_hom.z * p_w};
+            float s6[6];
+            const float2* c2 = reinterpret_cast<const float2*>(a.cov3d + 6 * (size_t)idx);
+            float2 c01 = __ldg(c2), c23 = __ldg(c2 + 1), c45 = __ldg(c2 + 2);
+            s6[0] = c01.x; s6[1] = c01.y; s6[2] = c23.x; s6[3] = c23.y; s6[4] = c45.x; s6[5] = c45.y;
+            float3 cov = cov2d(p_orig, a.fx, a.fy, a.tanx, a.tany, s6, a.view);
+            float det = (cov.x * cov.z - cov.y * cov.y);
+            float det_inv = 1.f / det;
+            conic = {cov.z * det_inv, -cov.y * det_inv, cov.x * det_inv};
+            log2_opacity = lg2_approx(opacity);
+            power = kLn2 * kCutoff + kLn2 * log2_opacity;
+            float trace = cov.x + cov.z;
+            if (2.0f * det * power < kBMinSq * trace && opacity < kOThin) break;
+            width = (int)(1.414214f * sqrt_approx(cov.x * power) + 1.0f);
+            height = (int)(1.414214f * sqrt_approx(cov.z * power) + 1.0f);
+            point_xy = {ndc_to_pix(p_proj.x, a.W), ndc_to_pix(p_proj.y, a.H)};
+            rect_min = {min(gridx, max(0, (int)((point_xy.x - width) / (float)a.bx))),
+                        min(gridy, max(0, (int)((point_xy.y - height) / (float)a.by)))};
+            rect_max = {min(gridx, max(0, (int)((point_xy.x + width) / (float)a.bx) + 1)),
+                        min(gridy, max(0, (int)((point_xy.y + height) / (float)a.by) + 1))};
+            point_valid = (rect_max.x - rect_min.x) * (rect_max.y - rect_min.y) > 0;
+        } while (false);
+    }
+
+    Stage st{s_keys[warp], s_vals[warp], 0};
+    const EmitOut out{a.keys, a.vals, a.cap, a.counter};
+    if (lane == 0) s_hit[warp] = 0u;
+    __syncwarp();
+    const uint32_t depth_bits = __float_as_uint(p_view.z);
+
+    // (1) single-tile Gaussians: one test per thread.
+    const int area = (rect_max.x - rect_min.x) * (rect_max.y - rect_min.y);
+    const bool single = point_valid && area == 1;
+    {
+        bool v = single && tile_hit(rect_min.x, rect_min.y, a.bx, a.by, point_xy, conic, power);
+        uint64_t key = ((uint64_t)(uint32_t)(rect_min.y * gridx + rect_min.x) << 32) | depth_bits;
+        stage_emit(st, out, v, key, (uint32_t)idx, lane);
+        unsigned m = __ballot_sync(GSR_FULL_MASK, v);
+        if (lane == 0 && m) atomicOr(&s_hit[warp], m);
+    }
+    point_valid = point_valid && !single;
+
+    // (2) multi-tile Gaussians: massive (whole warp per Gaussian over an 8x4
+    // tile window) or fragmented (flattened task pool), chosen per warp as in
+    // preprocess.cu:439-444.
+    const int my_tiles = point_valid ? area : 0;
+    const unsigned multi = __ballot_sync(GSR_FULL_MASK, point_valid);
+    const int multi_count = __popc(multi);
+    const int max_tiles = warp_max(my_tiles);
+    if (multi_count <= 2 || max_tiles >= 32) {
+        unsigned todo = multi;
+        while (todo) {
+            const int i = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const float2 c = {__shfl_sync(GSR_FULL_MASK, point_xy.x, i), __shfl_sync(GSR_FULL_MASK, point_xy.y, i)};
+            const float3 q = {__shfl_sync(GSR_FULL_MASK, conic.x, i), __shfl_sync(GSR_FULL_MASK, conic.y, i),
+                              __shfl_sync(GSR_FULL_MASK, conic.z, i)};
+            const int x_lo = __shfl_sync(GSR_FULL_MASK, rect_min.x, i), y_lo = __shfl_sync(GSR_FULL_MASK, rect_min.y, i);
+            const int x_hi = __shfl_sync(GSR_FULL_MASK, rect_max.x, i), y_hi = __shfl_sync(GSR_FULL_MASK, rect_max.y, i);
+            const uint32_t db = __shfl_sync(GSR_FULL_MASK, depth_bits, i);
+            const float pw = __shfl_sync(GSR_FULL_MASK, power, i);
+            const uint32_t gid = (uint32_t)(warp_first + i);
+            bool any = false;
+            for (int y0 = y_lo; y0 < y_hi; y0 += 4) {
+                const int y = y0 + ty;
+                for (int x0 = x_lo; x0 < x_hi; x0 += 8) {
+                    const int x = x0 + tx;
+                    bool v = y < y_hi && x < x_hi && tile_hit(x, y, a.bx, a.by, c, q, pw);
+                    any |= v;
+                    uint64_t key = ((uint64_t)(uint32_t)(y * gridx + x) << 32) | db;
+                    stage_emit(st, out, v, key, gid, lane);
+                }
+            }
+            if (__any_sync(GSR_FULL_MASK, any) && lane == 0) atomicOr(&s_hit[warp], 1u << i);
+        }
+    } else {
+        int prefix = my_tiles;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            int n = __shfl_up_sync(GSR_FULL_MASK, prefix, d);
+            if ((int)lane >= d) prefix += n;
+        }
+        const int total = __shfl_sync(GSR_FULL_MASK, prefix, 31);
+        prefix -= my_tiles;
+        const int default_owner = __ffs(multi) - 1;
+        for (int base = 0; base < total; base += 32) {
+            const int task = base + (int)lane;
+            const bool task_ok = task < total;
+            int owner = default_owner;
+            unsigned bits = multi;
+            while (bits) {
+                const int cand = __ffs(bits) - 1;
+                const int cp = __shfl_sync(GSR_FULL_MASK, prefix, cand);
+                const int cc = __shfl_sync(GSR_FULL_MASK, my_tiles, cand);
+                if (task_ok && task >= cp && task < cp + cc) owner = cand;
+                bits &= bits - 1;
+            }
+            const int ox = __shfl_sync(GSR_FULL_MASK, rect_min.x, owner);
+            const int oy = __shfl_sync(GSR_FULL_MASK, rect_min.y, owner);
+            const int ow = __shfl_sync(GSR_FULL_MASK, rect_max.x, owner) - ox;
+            const int op = __shfl_sync(GSR_FULL_MASK, prefix, owner);
+            const float2 c = {__shfl_sync(GSR_FULL_MASK, point_xy.x, owner),
+                              __shfl_sync(GSR_FULL_MASK, point_xy.y, owner)};
+            const float3 q = {__shfl_sync(GSR_FULL_MASK, conic.x, owner), __shfl_sync(GSR_FULL_MASK, conic.y, owner),
+                              __shfl_sync(GSR_FULL_MASK, conic.z, owner)};
+            const float pw = __shfl_sync(GSR_FULL_MASK, power, owner);
+            const uint32_t db = __shfl_sync(GSR_FULL_MASK, depth_bits, owner);
+            int x = 0, y = 0;
+            bool v = false;
+            if (task_ok) {
+                const int local = task - op;
+                const int row = ow > 0 ? local / ow : 0;
+                x = ox + (local - row * ow);
+                y = oy + row;
+                v = tile_hit(x, y, a.bx, a.by, c, q, pw);
+            }
+            uint64_t key = ((uint64_t)(uint32_t)(y * gridx + x) << 32) | db;
+            stage_emit(st, out, v, key, (uint32_t)(warp_first + owner), lane);
+            if (v) atomicOr(&s_hit[warp], 1u << owner);
+        }
+    }
+    __syncwarp();
+
+    // (3) render features for every Gaussian that emitted at least one key.
+    const bool emitted = (s_hit[warp] >> lane) & 1u;
+    if (emitted) {
+        a.points_xy[idx] = point_xy;
+        a.conic_opacity[idx] = make_float4((-0.5f * kLog2e) * conic.x, -kLog2e * conic.y, (-0.5f * kLog2e) * conic.z,
+                                           log2_opacity);
+        V3 cam = {a.campos[0], a.campos[1], a.campos[2]};
+        V3 col = sh_color<HALF>(idx, p_orig, cam, a.shs);
+        a.rgb_depth[idx] = make_float4(col.x, col.y, col.z, p_view.z);
+    }
+
+    // (4) block-wide final flush: one atomic per CTA.
+    if (lane == 0) s_fill[warp] = st.fill;
+    __syncthreads();
+    if (warp == 0) {
+        int f = lane < kWarps ? s_fill[lane] : 0;
+        int incl = f;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            int n = __shfl_up_sync(GSR_FULL_MASK, incl, d);
+            if ((int)lane >= d) incl += n;
+        }
+        int total = __shfl_sync(GSR_FULL_MASK, incl, 31);
+        long long base = 0;
+        if (lane == 0 && total > 0) base = atomicAdd(a.counter, total);
+        base = __shfl_sync(GSR_FULL_MASK, base, 0);
+        if (lane < kWarps) s_base[lane] = base + incl - f;
+    }
+    __syncthreads();
+    const long long wb = s_base[warp];
+    for (int i = lane; i < st.fill; i += 32) {
+        long long pos = wb + i;
+        if (pos < a.cap) {
+            a.keys[pos] = st.k[i];
+            a.vals[pos] = st.v[i];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Scene preparation (pybind.cpp:22-56, 105-117) on the device.
+__global__ void k_scene_prepare(int P, const float* __restrict__ log_scales, const float* __restrict__ quats,
+                                const float* __restrict__ logits, float* __restrict__ opacity,
+                                float* __restrict__ cov3d)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    opacity[i] = 1.0f / (1.0f + expf(-logits[i]));
+    float sx = expf(log_scales[3 * i]), sy = expf(log_scales[3 * i + 1]), sz = expf(log_scales[3 * i + 2]);
+    float4 q = reinterpret_cast<const float4*>(quats)[i];
+    float inv = rsqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+    float r = q.x * inv, x = q.y * inv, y = q.z * inv, z = q.w * inv;
+    M3 S = m3_cols(sx, 0.f, 0.f, 0.f, sy, 0.f, 0.f, 0.f, sz);
+    M3 R = m3_cols(1.f - 2.f * (y * y + z * z), 2.f * (x * y - r * z), 2.f * (x * z + r * y),
+                   2.f * (x * y + r * z), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - r * x),
+                   2.f * (x * z - r * y), 2.f * (y * z + r * x), 1.f - 2.f * (x * x + y * y));
+    M3 M = m3_mul(S, R);
+    M3 Sg = m3_mul(m3_transpose(M), M);
+    float* c = cov3d + 6 * (size_t)i;
+    c[0] = Sg.m[0][0];
+    c[1] = Sg.m[0][1];
+    c[2] = Sg.m[0][2];
+    c[3] = Sg.m[1][1];
+    c[4] = Sg.m[1][2];
+    c[5] = Sg.m[2][2];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side: view / projection matrices (preprocess.cu:643-671), column-major.
+
+static void mat4_mul(const float* a, const float* b, float* r)  // r = a * b, column-major
+{
+    for (int c = 0; c < 4; c++)
+        for (int k = 0; k < 4; k++)
+            r[4 * c + k] = a[0 * 4 + k] * b[4 * c + 0] + a[1 * 4 + k] * b[4 * c + 1] + a[2 * 4 + k] * b[4 * c + 2] +
+                           a[3 * 4 + k] * b[4 * c + 3];
+}
+
+void camera_matrices(int W, int H, const float* pos, const float* rot, float fx, float fy, float zfar, float znear,
+                     float* view, float* proj)
+{
+    // glm::mat3 built from the rows of `rot`: column c = rot row c.
+    float R[3][3];
+    for (int c = 0; c < 3; c++)
+        for (int k = 0; k < 3; k++) R[c][k] = rot[3 * c + k];
+    float np[3] = {-pos[0], -pos[1], -pos[2]};
+    float t[3];
+    for (int k = 0; k < 3; k++) t[k] = R[0][k] * np[0] + R[1][k] * np[1] + R[2][k] * np[2];
+    for (int c = 0; c < 3; c++) {
+        for (int k = 0; k < 3; k++) view[4 * c + k] = R[c][k];
+        view[4 * c + 3] = 0.0f;
+    }
+    view[12] = t[0];
+    view[13] = t[1];
+    view[14] = t[2];
+    view[15] = 1.0f;
+
+    float top = H / (2.0f * fy) * znear;
+    float bottom = -top;
+    float right = W / (2.0f * fx) * znear;
+    float left = -right;
+    float P[16];
+    for (int i = 0; i < 16; i++) P[i] = 0.0f;
+    const float z_sign = 1.0f;
+    P[0 * 4 + 0] = 2.0f * znear / (right - left);
+    P[1 * 4 + 1] = 2.0f * znear / (top - bottom);
+    P[0 * 4 + 2] = (right + left) / (right - left);
+    P[1 * 4 + 2] = (top + bottom) / (top - bottom);
+    P[3 * 4 + 2] = z_sign;
+    P[2 * 4 + 2] = z_sign * zfar / (zfar - znear);
+    P[2 * 4 + 3] = -(zfar * znear) / (zfar - znear);
+    float PT[16];
+    for (int c = 0; c < 4; c++)
+        for (int k = 0; k < 4; k++) PT[4 * c + k] = P[4 * k + c];
+    mat4_mul(PT, view, proj);
+}
+
+cudaError_t launch_scene_prepare(int P, const float* log_scales, const float* quats, const float* logits,
+                                 float* opacity, float* cov3d, cudaStream_t stream)
+{
+    if (P <= 0) return cudaSuccess;
+    k_scene_prepare<<<div_up(P, 256), 256, 0, stream>>>(P, log_scales, quats, logits, opacity, cov3d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_preprocess(const PreprocessParams& p, bool half_sh, cudaStream_t stream)
+{
+    if (p.P <= 0) return cudaSuccess;
+    const int grid = div_up(p.P, kThreads);
+    if (half_sh) k_preprocess<true><<<grid, kThreads, 0, stream>>>(p);
+    else k_preprocess<false><<<grid, kThreads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace gsr

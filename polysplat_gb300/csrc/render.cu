@@ -1,0 +1,409 @@
+// Persistent tile-queue blend for sm_103a.
+//
+// One warp renders one tile at a time; every lane owns a (BX/8) x (BY/4)
+// block of pixels (8 x 4 lanes over the tile, csrc/cuda_rasterizer/
+// render.cu:1736-1737).  Warps take tiles from a per-launch atomic queue in
+// the caller's workspace (no module-global counter, so concurrent launches on
+// different workspaces are safe).  The Gaussians of a tile are consumed in
+// batches of 32: for each batch every lane issues 1-D TMA bulk copies
+// (cp.async.bulk) of its Gaussian's conic/opacity, colour/depth and centre
+// records into one half of a double-buffered shared-memory ring whose
+// completion is tracked by an mbarrier transaction count, so the next batch
+// streams in while the current one is blended.  Every wait is bounded: on
+// expiry the warp records a timeout in the status word and stops.
+//
+// The blend of each Gaussian-pixel pair is the reference's arithmetic
+// (pixel_shader_axis_shared_16x16 / pixel_shader, render.cu:228-271 and
+// 216-226): alpha = ex2.approx.ftz(power) with no 0.99 clamp and no 1/255
+// skip, front-to-back compositing, and a whole-tile exit once every pixel of
+// the tile has T < 1e-4, checked every CADENCE Gaussians.  Output is the
+// truncating uint8 encode of render.cu:375-394.
+#include "gsr_internal.h"
+
+namespace gsr {
+namespace {
+
+constexpr int kRenderWarps = 4;
+constexpr int kBatch = 32;
+
+struct WarpRing {
+    float4 con[2][kBatch];
+    float4 rgbd[2][kBatch];
+    float4 xy2[2][kBatch];  // 16-byte pair holding the Gaussian's centre
+    uint32_t sel[2][kBatch];
+    uint64_t bar[2];
+};
+
+struct RenderParams {
+    int n_host;
+    const int32_t* d_num;
+    long long cap;
+    int W, H, gx, tiles, P;
+    const float2* xy;
+    const float4* rgbd;
+    const float4* con;
+    const uint64_t* keys;
+    const uint32_t* vals;
+    const int2* ranges;
+    float3 bg;
+    uchar3* out;
+    uint32_t* queue;
+    uint32_t* status;
+};
+
+__device__ __forceinline__ uint8_t encode8(float x) { return (uint8_t)fminf(fmaxf(0.0f, x * 255.0f), 255.0f); }
+
+// First index in keys[lo, hi) whose tile id is > t (UPPER) or >= t (!UPPER);
+// warp-cooperative 32-way search, log32(n) rounds.
+template <bool UPPER>
+__device__ __forceinline__ int warp_bound(const uint64_t* __restrict__ keys, int lo, int hi, uint32_t t, unsigned lane)
+{
+    while (hi - lo > 32) {
+        const int step = (hi - lo + 31) >> 5;
+        const int p = lo + ((int)lane + 1) * step - 1;
+        bool pred = false;
+        if (p < hi) {
+            const uint32_t kt = (uint32_t)(__ldg(keys + p) >> 32);
+            pred = UPPER ? (kt <= t) : (kt < t);
+        }
+        const int c = __popc(__ballot_sync(GSR_FULL_MASK, pred));
+        const int nlo = c == 0 ? lo : lo + c * step;  // first probe that failed is p_c
+        const int nhi = min(hi, lo + (c + 1) * step);
+        lo = nlo;
+        hi = nhi;
+    }
+    const int p = lo + (int)lane;
+    bool pred = false;
+    if (p < hi) {
+        const uint32_t kt = (uint32_t)(__ldg(keys + p) >> 32);
+        pred = UPPER ? (kt <= t) : (kt < t);
+    }
+    return lo + __popc(__ballot_sync(GSR_FULL_MASK, pred));
+}
+
+// Stage Gaussians vals[pos, pos+cnt) into ring half `b`.
+template <bool TMA>
+__device__ __forceinline__ void stage_batch(WarpRing& R, int b, const RenderParams& p, int pos, int cnt,
+                                            unsigned lane, bool& bad)
+{
+    __syncwarp();
+    if (TMA) fence_proxy_async_smem();
+    uint32_t gid = 0;
+    bool ok = (int)lane < cnt;
+    if (ok) {
+        gid = __ldg(p.vals + pos + lane);
+        if (gid >= (uint32_t)p.P) {  // index outside the feature arrays: skip it
+            ok = false;
+            bad = true;
+        }
+    }
+    const bool pair_ok = ok && (gid | 1u) < (uint32_t)p.P;
+    if (TMA) {
+        const uint32_t tx = 32u * __popc(__ballot_sync(GSR_FULL_MASK, ok)) + 16u * __popc(__ballot_sync(GSR_FULL_MASK, pair_ok));
+        if (lane == 0) mbar_arrive_expect_tx(&R.bar[b], tx);
+        __syncwarp();
+        if (ok) {
+            tma_bulk_g2s(&R.con[b][lane], p.con + gid, 16, &R.bar[b]);
+            tma_bulk_g2s(&R.rgbd[b][lane], p.rgbd + gid, 16, &R.bar[b]);
+            if (pair_ok) {
+                tma_bulk_g2s(&R.xy2[b][lane], p.xy + (gid & ~1u), 16, &R.bar[b]);
+                R.sel[b][lane] = gid & 1u;
+            } else {
+                const float2 v = __ldg(p.xy + gid);
+                R.xy2[b][lane] = make_float4(v.x, v.y, 0.f, 0.f);
+                R.sel[b][lane] = 0u;
+            }
+        }
+        if (!ok && (int)lane < cnt) {  // skipped index: a fully transparent stand-in
+            R.con[b][lane] = make_float4(0.f, 0.f, 0.f, -1e30f);
+            R.rgbd[b][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+            R.xy2[b][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+            R.sel[b][lane] = 0u;
+        }
+    } else {
+        if (ok) {
+            cp_async_16(&R.con[b][lane], p.con + gid);
+            cp_async_16(&R.rgbd[b][lane], p.rgbd + gid);
+            cp_async_8(&R.xy2[b][lane], p.xy + gid);
+            R.sel[b][lane] = 0u;
+        } else if ((int)lane < cnt) {
+            R.con[b][lane] = make_float4(0.f, 0.f, 0.f, -1e30f);
+            R.rgbd[b][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+            R.xy2[b][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+            R.sel[b][lane] = 0u;
+        }
+        cp_async_commit();
+    }
+}
+
+// Wait until ring half `b` is filled.  Returns false on timeout.
+template <bool TMA>
+__device__ __forceinline__ bool wait_batch(WarpRing& R, int b, uint32_t& phase_bits)
+{
+    bool ok = true;
+    if (TMA) {
+        ok = mbar_wait_bounded(&R.bar[b], (phase_bits >> b) & 1u);
+        phase_bits ^= 1u << b;
+    } else {
+        cp_async_wait_all();
+    }
+    __syncwarp();
+    return ok;
+}
+
+// SHADER 0: pixel_shader_axis_shared_16x16 (render.cu:228-271)
+// SHADER 1: pixel_shader (render.cu:216-226)
+template <int TX, int TY, int SHADER, bool DT>
+__device__ __forceinline__ void shade(float (&C)[TY][TX][3], float (&T)[TY][TX], int ox, int oy, int cb, int rb,
+                                      float2 xy, float4 co, float3 rgb)
+{
+    if (SHADER == 0) {
+        float xs[TX], xc[TX];
+#pragma unroll
+        for (int j = 0; j < TX; j++) {
+            float dx = xy.x - (float)(ox + cb + j);
+            xs[j] = co.x * dx * dx;
+            xc[j] = co.y * dx;
+        }
+        float yd[TY], ys[TY];
+#pragma unroll
+        for (int i = 0; i < TY; i++) {
+            float dy = xy.y - (float)(oy + rb + i);
+            yd[i] = dy;
+            ys[i] = co.z * dy * dy;
+        }
+#pragma unroll
+        for (int i = 0; i < TY; i++)
+#pragma unroll
+            for (int j = 0; j < TX; j++) {
+                float power = fmaf(xc[j], yd[i], co.w + xs[j] + ys[i]);
+                if (DT && !(power >= -7.994353375f)) continue;
+                float alpha = ex2_approx_ftz(power);
+                float weight = alpha * T[i][j];
+                C[i][j][0] += rgb.x * weight;
+                C[i][j][1] += rgb.y * weight;
+                C[i][j][2] += rgb.z * weight;
+                T[i][j] -= weight;
+            }
+    } else {
+#pragma unroll
+        for (int i = 0; i < TY; i++)
+#pragma unroll
+            for (int j = 0; j < TX; j++) {
+                float dx = xy.x - (float)(ox + cb + j);
+                float dy = xy.y - (float)(oy + rb + i);
+                float power = co.w + co.x * dx * dx + co.z * dy * dy + co.y * dx * dy;
+                float alpha = ex2_approx_ftz(power);
+                C[i][j][0] += rgb.x * (alpha * T[i][j]);
+                C[i][j][1] += rgb.y * (alpha * T[i][j]);
+                C[i][j][2] += rgb.z * (alpha * T[i][j]);
+                T[i][j] -= alpha * T[i][j];
+            }
+    }
+}
+
+// RANGE_MODE 0: ranges[] given; 1: warp search in the sorted keys.
+template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA>
+__global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams p)
+{
+    constexpr int TX = BX / 8, TY = BY / 4;
+    __shared__ WarpRing rings[kRenderWarps];
+    const unsigned lane = threadIdx.x & 31u;
+    const int warp = threadIdx.x >> 5;
+    WarpRing& R = rings[warp];
+    if (TMA) {
+        if (lane == 0) {
+            mbar_init(&R.bar[0], 1);
+            mbar_init(&R.bar[1], 1);
+            fence_mbar_init();
+        }
+        __syncwarp();
+    }
+    long long nl = p.d_num ? (long long)*p.d_num : (long long)p.n_host;
+    const int n = (int)max(0LL, min(nl, p.cap));
+    const int cb = (int)(lane & 7u) * TX;
+    const int rb = (int)(lane >> 3) * TY;
+    uint32_t phase_bits = 0;
+    bool bad = false;
+    bool timed_out = false;
+
+    int tile = blockIdx.x * kRenderWarps + warp;
+    while (tile < p.tiles) {
+        const int ox = (tile % p.gx) * BX;
+        const int oy = (tile / p.gx) * BY;
+        int start, end;
+        if (RANGE_MODE == 0) {
+            int2 r = make_int2(0, 0);
+            if (lane == 0) r = __ldg(p.ranges + tile);
+            // ranges come from the caller: keep them inside [0, n]
+            start = min(max(__shfl_sync(GSR_FULL_MASK, r.x, 0), 0), n);
+            end = min(max(__shfl_sync(GSR_FULL_MASK, r.y, 0), start), n);
+        } else {
+            start = warp_bound<false>(p.keys, 0, n, (uint32_t)tile, lane);
+            end = warp_bound<true>(p.keys, start, n, (uint32_t)tile, lane);
+        }
+        float T[TY][TX];
+        float C[TY][TX][3];
+#pragma unroll
+        for (int i = 0; i < TY; i++)
+#pragma unroll
+            for (int j = 0; j < TX; j++) {
+                T[i][j] = 1.0f;
+                C[i][j][0] = C[i][j][1] = C[i][j][2] = 0.0f;
+            }
+        const int total = end - start;
+        if (total > 0) {
+            int cur = 0;
+            stage_batch<TMA>(R, 0, p, start, min(kBatch, total), lane, bad);
+            int processed = 0;
+            for (int pos = start; pos < end; pos += kBatch) {
+                const int bsize = min(kBatch, end - pos);
+                const int npos = pos + kBatch;
+                const int nsize = max(0, min(kBatch, end - npos));
+                if (!wait_batch<TMA>(R, cur, phase_bits)) {
+                    timed_out = true;
+                    break;
+                }
+                if (nsize > 0) stage_batch<TMA>(R, cur ^ 1, p, npos, nsize, lane, bad);
+                bool exit_now = false;
+                for (int g = 0; g < bsize; g++) {
+                    const float4 co = R.con[cur][g];
+                    const float4 cd = R.rgbd[cur][g];
+                    const float4 x2 = R.xy2[cur][g];
+                    const float2 xy = R.sel[cur][g] ? make_float2(x2.z, x2.w) : make_float2(x2.x, x2.y);
+                    shade<TX, TY, SHADER, DT>(C, T, ox, oy, cb, rb, xy, co, make_float3(cd.x, cd.y, cd.z));
+                    ++processed;
+                    if (processed % CADENCE == 0) {
+                        bool sat = true;
+#pragma unroll
+                        for (int i = 0; i < TY; i++)
+#pragma unroll
+                            for (int j = 0; j < TX; j++) sat = sat && T[i][j] < 0.0001f;
+                        if (__all_sync(GSR_FULL_MASK, sat)) {
+                            exit_now = true;
+                            break;
+                        }
+                    }
+                }
+                cur ^= 1;
+                if (exit_now) {
+                    // consume the batch already in flight so the ring is idle
+                    if (nsize > 0 && !wait_batch<TMA>(R, cur, phase_bits)) timed_out = true;
+                    break;
+                }
+            }
+        }
+        if (timed_out) break;
+#pragma unroll
+        for (int i = 0; i < TY; i++)
+#pragma unroll
+            for (int j = 0; j < TX; j++) {
+                const int px = ox + cb + j, py = oy + rb + i;
+                if (px < p.W && py < p.H) {
+                    float t = T[i][j];
+                    if (t < 0.0001f) t = 0.0f;
+                    uchar3 o;
+                    if (total > 0) {
+                        o.x = encode8(C[i][j][0] + t * p.bg.x);
+                        o.y = encode8(C[i][j][1] + t * p.bg.y);
+                        o.z = encode8(C[i][j][2] + t * p.bg.z);
+                    } else {
+                        o.x = encode8(p.bg.x);
+                        o.y = encode8(p.bg.y);
+                        o.z = encode8(p.bg.z);
+                    }
+                    p.out[(size_t)py * p.W + px] = o;
+                }
+            }
+        int next = 0;
+        if (lane == 0) next = (int)atomicAdd(p.queue, 1u) + (int)gridDim.x * kRenderWarps;
+        tile = __shfl_sync(GSR_FULL_MASK, next, 0);
+    }
+    if (timed_out && lane == 0) record_error(p.status, kErrTimeout);
+    if (__any_sync(GSR_FULL_MASK, bad) && lane == 0) record_error(p.status, kErrBadInput);
+    if (TMA && timed_out) {
+        // give copies still in flight a bounded chance to land before exit
+        mbar_wait_bounded(&R.bar[0], (phase_bits >> 0) & 1u);
+        mbar_wait_bounded(&R.bar[1], (phase_bits >> 1) & 1u);
+    }
+}
+
+template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA>
+cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
+{
+    auto kern = k_render<BX, BY, CADENCE, SHADER, DT, RANGE_MODE, TMA>;
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kRenderWarps * 32, 0) != cudaSuccess || b < 1) b = 1;
+        per_sm = b;
+    }
+    const int warps_needed = p.tiles;
+    int grid = device_sm_count() * per_sm;
+    grid = max(1, min(grid, div_up(warps_needed, kRenderWarps)));
+    kern<<<grid, kRenderWarps * 32, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+template <int BX, int BY>
+cudaError_t dispatch_shape(int variant, bool tma, const RenderParams& p, cudaStream_t stream)
+{
+    constexpr int SH = (BX == 16 && BY == 16) ? 0 : 1;
+    switch (variant) {
+    case GSR_RENDER_PERSISTENT_RANGES:
+        return tma ? launch_variant<BX, BY, 8, 0, false, 0, true>(p, stream)
+                   : launch_variant<BX, BY, 8, 0, false, 0, false>(p, stream);
+    case GSR_RENDER_PERSISTENT_FUSED:
+        return tma ? launch_variant<BX, BY, 16, 0, false, 1, true>(p, stream)
+                   : launch_variant<BX, BY, 16, 0, false, 1, false>(p, stream);
+    case GSR_RENDER_DEFAULT:
+        return tma ? launch_variant<BX, BY, 2, SH, false, 1, true>(p, stream)
+                   : launch_variant<BX, BY, 2, SH, false, 1, false>(p, stream);
+    case GSR_RENDER_RANGES_CADENCE2:
+        return tma ? launch_variant<BX, BY, 2, SH, false, 0, true>(p, stream)
+                   : launch_variant<BX, BY, 2, SH, false, 0, false>(p, stream);
+    case GSR_RENDER_DT:
+        return tma ? launch_variant<BX, BY, 8, 0, true, 0, true>(p, stream)
+                   : launch_variant<BX, BY, 8, 0, true, 0, false>(p, stream);
+    default:
+        return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream)
+{
+    RenderParams p;
+    p.n_host = a.num;
+    p.d_num = a.d_num;
+    p.cap = a.d_num ? a.cap : (long long)a.num;
+    p.W = a.W;
+    p.H = a.H;
+    p.gx = div_up(a.W, a.bx);
+    p.tiles = p.gx * div_up(a.H, a.by);
+    p.P = a.P;
+    p.xy = a.xy;
+    p.rgbd = a.rgbd;
+    p.con = a.con;
+    p.keys = a.keys;
+    p.vals = a.vals;
+    p.ranges = a.ranges;
+    p.bg = make_float3(a.bg[0], a.bg[1], a.bg[2]);
+    p.out = reinterpret_cast<uchar3*>(a.out);
+    p.queue = &a.ws->render_queue;
+    p.status = &a.ws->status;
+    if (p.tiles <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(p.queue, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
+    // TMA bulk copies need 16-byte aligned feature arrays.
+    const bool tma = ((reinterpret_cast<uintptr_t>(a.xy) | reinterpret_cast<uintptr_t>(a.rgbd) |
+                       reinterpret_cast<uintptr_t>(a.con)) & 15u) == 0;
+    if (a.bx == 16 && a.by == 16) return dispatch_shape<16, 16>(a.variant, tma, p, stream);
+    if (a.bx == 32 && a.by == 16) return dispatch_shape<32, 16>(a.variant, tma, p, stream);
+    if (a.bx == 24 && a.by == 16) return dispatch_shape<24, 16>(a.variant, tma, p, stream);
+    if (a.bx == 32 && a.by == 32) return dispatch_shape<32, 32>(a.variant, tma, p, stream);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace gsr

@@ -1,0 +1,360 @@
+// Stable LSD radix sort of (u64 key, u32 value) pairs for sm_103a.
+//
+// Contract (same as the reference's CUB call, csrc/cuda_rasterizer/sort.cu:
+// 107-125): ascending, stable, unsigned, over bits [0, end_bit); bits at or
+// above end_bit ride along but do not take part in the order; the inputs are
+// preserved.  The count may live on the device, so no host synchronisation
+// is needed between the producer of the keys and the sort.
+//
+// Structure (one-sweep radix sort with decoupled look-back):
+//   1. k_upsweep: one read of all keys builds the 256-bin histogram of every
+//      8-bit digit pass at once, and clears the first look-back array.
+//   2. k_pass (one launch per digit): persistent CTAs take 4096-key tiles in
+//      order from an atomic counter, rank keys stably inside the tile (per-warp
+//      ballot ranking), publish per-digit tile counts, look back over earlier
+//      tiles for the running per-digit prefix (bounded spin), reorder the tile
+//      in shared memory by digit and write it out with coalesced stores.
+#include <algorithm>
+
+#include "gsr_internal.h"
+
+namespace gsr {
+namespace {
+
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagPrefix = 2u << 30;
+constexpr uint32_t kValueMask = (1u << 30) - 1u;
+constexpr int kWarpsPerCta = kSortThreads / 32;
+constexpr int kWarpItems = kSortItems * 32;  // 512 consecutive keys per warp
+
+__device__ __forceinline__ int sort_count(const SortArgs& a)
+{
+    long long n = a.d_num ? (long long)*a.d_num : (long long)a.num;
+    if (n < 0) n = 0;
+    if (n > a.cap) n = a.cap;
+    return (int)n;
+}
+
+struct Layout {
+    WorkspaceHeader* hdr;
+    uint64_t* alt_keys;
+    uint32_t* alt_vals;
+    uint32_t* look[2];
+    long long tiles_cap;
+};
+
+__host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+__host__ __device__ inline Layout make_layout(void* ws, long long cap)
+{
+    Layout L;
+    char* p = reinterpret_cast<char*>(ws);
+    L.hdr = reinterpret_cast<WorkspaceHeader*>(p);
+    size_t off = kHeaderBytes;
+    L.alt_keys = reinterpret_cast<uint64_t*>(p + off);
+    off += align256((size_t)cap * 8);
+    L.alt_vals = reinterpret_cast<uint32_t*>(p + off);
+    off += align256((size_t)cap * 4);
+    L.tiles_cap = (cap + kSortTile - 1) / kSortTile;
+    L.look[0] = reinterpret_cast<uint32_t*>(p + off);
+    off += align256((size_t)L.tiles_cap * 256 * 4);
+    L.look[1] = reinterpret_cast<uint32_t*>(p + off);
+    return L;
+}
+
+// ---------------------------------------------------------------------------
+// Histogram of every digit pass.  Each thread takes runs of 8 consecutive keys
+// and merges equal consecutive digits before touching shared memory: keys of
+// one Gaussian are emitted together and share their depth digits, so this
+// removes most same-address shared atomics.
+__global__ __launch_bounds__(256) void k_upsweep(SortArgs a, Layout L, int passes)
+{
+    __shared__ uint32_t s_hist[kMaxPasses][256];
+    for (int i = threadIdx.x; i < kMaxPasses * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0u;
+    __syncthreads();
+    const int n = sort_count(a);
+    const int tiles = (n + kSortTile - 1) / kSortTile;
+    // clear the look-back state used by the first digit pass
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)tiles * 256;
+         i += (long long)gridDim.x * blockDim.x)
+        L.look[0][i] = 0u;
+
+    const long long runs = (n + 7) / 8;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < runs;
+         r += (long long)gridDim.x * blockDim.x) {
+        const long long b = r * 8;
+        uint64_t k[8];
+        const int cnt = (int)min(8LL, (long long)n - b);
+        if (cnt == 8 && ((reinterpret_cast<uintptr_t>(a.keys_in + b) & 15) == 0)) {
+            const uint4* src = reinterpret_cast<const uint4*>(a.keys_in + b);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                uint4 v = __ldg(src + j);
+                k[2 * j] = ((uint64_t)v.y << 32) | v.x;
+                k[2 * j + 1] = ((uint64_t)v.w << 32) | v.z;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; j++) k[j] = j < cnt ? __ldg(a.keys_in + b + j) : 0ull;
+        }
+        for (int p = 0; p < passes; p++) {
+            const int shift = 8 * p;
+            const int bits = min(8, a.end_bit - shift);
+            const uint32_t mask = (1u << bits) - 1u;
+            uint32_t cur = (uint32_t)(k[0] >> shift) & mask;
+            uint32_t run = 1;
+#pragma unroll
+            for (int j = 1; j < 8; j++) {
+                if (j >= cnt) break;
+                uint32_t d = (uint32_t)(k[j] >> shift) & mask;
+                if (d == cur) {
+                    run++;
+                } else {
+                    atomicAdd(&s_hist[p][cur], run);
+                    cur = d;
+                    run = 1;
+                }
+            }
+            atomicAdd(&s_hist[p][cur], run);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
+        uint32_t v = (&s_hist[0][0])[i];
+        if (v) atomicAdd(&L.hdr->hist[0][0] + i, v);
+    }
+}
+
+// ---------------------------------------------------------------------------
+struct PassSmem {
+    uint64_t keys[kSortTile];
+    uint32_t vals[kSortTile];
+    uint32_t whist[kWarpsPerCta][256];  // per-warp digit counts, then warp-exclusive offsets
+    uint32_t digit_excl[256];           // tile-local start of each digit
+    int gofs[256];                      // global position of tile position 0 per digit
+    uint32_t gstart[256];               // global start of each digit (scan of histogram)
+    uint32_t warp_sums[kWarpsPerCta];
+    int tile;
+};
+
+// Exclusive scan of 256 values held one per thread (blockDim == 256).
+__device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* warp_sums, uint32_t& total)
+{
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t n = __shfl_up_sync(GSR_FULL_MASK, incl, d);
+        if (lane >= (unsigned)d) incl += n;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    uint32_t wpre = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < kWarpsPerCta; w++) {
+        uint32_t s = warp_sums[w];
+        if (w < (int)warp) wpre += s;
+        tot += s;
+    }
+    total = tot;
+    __syncthreads();
+    return wpre + incl - v;
+}
+
+__global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortArgs a, Layout L, int pass, int passes,
+                                                          const uint64_t* __restrict__ kin,
+                                                          const uint32_t* __restrict__ vin, uint64_t* kout,
+                                                          uint32_t* vout)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PassSmem& S = *reinterpret_cast<PassSmem*>(smem_raw);
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const int n = sort_count(a);
+    const int tiles = (n + kSortTile - 1) / kSortTile;
+    const int shift = 8 * pass;
+    const int bits = min(8, a.end_bit - shift);
+    const uint32_t dmask = (1u << bits) - 1u;
+    uint32_t* look = L.look[pass & 1];
+    uint32_t* look_next = L.look[(pass + 1) & 1];
+    const bool clear_next = pass + 1 < passes;
+
+    // global digit starts for this pass
+    {
+        uint32_t tot;
+        uint32_t h = L.hdr->hist[pass][threadIdx.x];
+        S.gstart[threadIdx.x] = block_excl_scan256(h, S.warp_sums, tot);
+    }
+
+    for (;;) {
+        if (threadIdx.x == 0) S.tile = (int)atomicAdd(&L.hdr->pass_counter[pass], 1u);
+        __syncthreads();
+        const int tile = S.tile;
+        if (tile >= tiles) break;
+        const long long tbase = (long long)tile * kSortTile;
+        const int tcount = (int)min((long long)kSortTile, (long long)n - tbase);
+        if (clear_next) look_next[(size_t)tile * 256 + threadIdx.x] = 0u;
+
+        // ---- load + rank (warp-contiguous chunk of 512 keys) ----
+        for (int i = threadIdx.x; i < kWarpsPerCta * 256; i += kSortThreads) (&S.whist[0][0])[i] = 0u;
+        __syncwarp();
+        __syncthreads();
+        uint64_t key[kSortItems];
+        uint32_t val[kSortItems];
+        uint32_t rank[kSortItems];
+        const int wbase = (int)warp * kWarpItems;
+#pragma unroll
+        for (int i = 0; i < kSortItems; i++) {
+            const int o = wbase + i * 32 + (int)lane;
+            if (o < tcount) {
+                key[i] = kin[tbase + o];
+                val[i] = vin[tbase + o];
+            } else {
+                key[i] = 0ull;
+                val[i] = 0u;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < kSortItems; i++) {
+            const int o = wbase + i * 32 + (int)lane;
+            const bool ok = o < tcount;
+            const uint32_t d = (uint32_t)(key[i] >> shift) & dmask;
+            unsigned peers = __ballot_sync(GSR_FULL_MASK, ok);
+            for (int b = 0; b < bits; b++) {
+                const bool bit = (d >> b) & 1u;
+                const unsigned bb = __ballot_sync(GSR_FULL_MASK, bit);
+                peers &= bit ? bb : ~bb;
+            }
+            uint32_t base = 0;
+            if (ok) base = S.whist[warp][d];
+            __syncwarp();
+            if (ok && (lane == (unsigned)(__ffs(peers) - 1))) S.whist[warp][d] = base + __popc(peers);
+            __syncwarp();
+            rank[i] = base + __popc(peers & lanemask_lt());
+        }
+        __syncthreads();
+
+        // ---- per-digit offsets: across warps, then across digits ----
+        uint32_t dtot;
+        {
+            const int d = threadIdx.x;
+            uint32_t run = 0;
+#pragma unroll
+            for (int w = 0; w < kWarpsPerCta; w++) {
+                uint32_t c = S.whist[w][d];
+                S.whist[w][d] = run;
+                run += c;
+            }
+            dtot = run;
+            uint32_t total;
+            S.digit_excl[d] = block_excl_scan256(run, S.warp_sums, total);
+        }
+
+        // ---- decoupled look-back: thread d owns digit d ----
+        {
+            const int d = threadIdx.x;
+            uint32_t* my = look + (size_t)tile * 256 + d;
+            st_relaxed_u32(my, (tile == 0 ? kFlagPrefix : kFlagAgg) | dtot);
+            uint32_t excl = 0;
+            for (int j = tile - 1; j >= 0; j--) {
+                const uint32_t* p = look + (size_t)j * 256 + d;
+                uint32_t v = ld_relaxed_u32(p);
+                uint32_t spins = 0;
+                while ((v & ~kValueMask) == 0u) {
+                    if (++spins > kSpinLimit) {
+                        record_error(&L.hdr->status, kErrTimeout);
+                        break;
+                    }
+                    __nanosleep(32);
+                    v = ld_relaxed_u32(p);
+                }
+                excl += v & kValueMask;
+                if ((v & kFlagPrefix) || (v & ~kValueMask) == 0u) break;
+            }
+            if (tile != 0) st_relaxed_u32(my, kFlagPrefix | ((excl + dtot) & kValueMask));
+            S.gofs[d] = (int)(S.gstart[d] + excl) - (int)S.digit_excl[d];
+        }
+        __syncthreads();
+
+        // ---- reorder in shared memory, then coalesced scatter ----
+#pragma unroll
+        for (int i = 0; i < kSortItems; i++) {
+            const int o = wbase + i * 32 + (int)lane;
+            if (o < tcount) {
+                const uint32_t d = (uint32_t)(key[i] >> shift) & dmask;
+                const uint32_t pos = S.digit_excl[d] + S.whist[warp][d] + rank[i];
+                S.keys[pos] = key[i];
+                S.vals[pos] = val[i];
+            }
+        }
+        __syncthreads();
+        bool oob = false;
+        for (int p = threadIdx.x; p < tcount; p += kSortThreads) {
+            const uint64_t k = S.keys[p];
+            const uint32_t d = (uint32_t)(k >> shift) & dmask;
+            const long long g = (long long)S.gofs[d] + p;
+            if (g < 0 || g >= n) {  // only after a look-back timeout: never write outside the buffer
+                oob = true;
+                continue;
+            }
+            kout[g] = k;
+            vout[g] = S.vals[p];
+        }
+        if (oob) record_error(&L.hdr->status, kErrTimeout);
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+size_t sort_workspace_bytes(long long cap)
+{
+    if (cap < 1) cap = 1;
+    long long tiles = (cap + kSortTile - 1) / kSortTile;
+    return kHeaderBytes + align256((size_t)cap * 8) + align256((size_t)cap * 4) + 2 * align256((size_t)tiles * 256 * 4);
+}
+
+cudaError_t launch_sort(const SortArgs& a, cudaStream_t stream)
+{
+    if (a.end_bit < 1 || a.end_bit > 64) return cudaErrorInvalidValue;
+    if (a.ws_bytes < sort_workspace_bytes(a.cap)) return cudaErrorInvalidValue;
+    if (a.cap >= (1LL << 30)) return cudaErrorInvalidValue;
+    Layout L = make_layout(a.ws, a.cap);
+    const int passes = (a.end_bit + 7) / 8;
+    // clear counters and histograms, keep the status word
+    cudaError_t e = cudaMemsetAsync(reinterpret_cast<char*>(L.hdr) + sizeof(uint32_t), 0,
+                                    sizeof(WorkspaceHeader) - sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
+    const int sms = device_sm_count();
+    const long long tiles_cap = L.tiles_cap;
+    int up_grid = (int)std::min<long long>((long long)sms * 4, std::max<long long>(1, (a.cap + 2047) / 2048));
+    k_upsweep<<<up_grid, 256, 0, stream>>>(a, L, passes);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+
+    static bool attr_set = false;
+    const int smem = (int)sizeof(PassSmem);
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr_set = true;
+    }
+    const int grid = (int)std::min<long long>((long long)sms * 2, std::max<long long>(1, tiles_cap));
+    for (int p = 0; p < passes; p++) {
+        const bool to_out = ((passes - 1 - p) % 2) == 0;
+        const uint64_t* kin;
+        const uint32_t* vin;
+        if (p == 0) {
+            kin = a.keys_in;
+            vin = a.vals_in;
+        } else {
+            const bool prev_out = ((passes - p) % 2) == 0;
+            kin = prev_out ? a.keys_out : L.alt_keys;
+            vin = prev_out ? a.vals_out : L.alt_vals;
+        }
+        uint64_t* ko = to_out ? a.keys_out : L.alt_keys;
+        uint32_t* vo = to_out ? a.vals_out : L.alt_vals;
+        k_pass<<<grid, kSortThreads, smem, stream>>>(a, L, p, passes, kin, vin, ko, vo);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace gsr

@@ -1,0 +1,309 @@
+"""GPU parity: the sm_103a CUDA path (through the drop-in ops and the C ABI)
+against the FP64 CPU oracle on the same seeded inputs.
+
+Bars: bit-exact for the integer stages (sort, tile ranges, gather); for the
+floating-point stages the tolerances are written beside each assert:
+  * preprocess: (tile, Gaussian) pair sets equal up to ellipse-boundary flips
+    (<= 1e-4 of M, at least 8), depth bits within 2 ulp, features within
+    rel 2e-4 (fast-math lg2/rsqrt/sqrt vs exact FP64);
+  * images: max-abs <= 2/255 and PSNR >= 50 dB.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from polysplat_gb300 import Camera, Rasterizer, Scene, ops, scenes
+from polysplat_gb300._lib import GsrError, lib
+
+from helpers import (compare_key_lists, image_stats, random_tile_keys, values_equal_within_key_runs)
+
+pytestmark = pytest.mark.gpu
+
+
+def _t(a, dev, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.to(dev)
+
+
+def _keys_t(keys, dev):
+    return torch.from_numpy(keys.view(np.int64).copy()).to(dev)
+
+
+def _np_keys(t):
+    return t.cpu().numpy().view(np.uint64)
+
+
+def _np_vals(t):
+    return t.cpu().numpy().view(np.uint32)
+
+
+# ---------------------------------------------------------------------------- sort
+
+@pytest.mark.parametrize("n", [0, 1, 31, 4095, 4096, 4097, 65537, 1_000_003])
+@pytest.mark.parametrize("end_bit", [43, 45, 49, 64])
+def test_sort_bit_exact(cuda_device, n, end_bit):
+    rng = np.random.default_rng(1000 * n + end_bit)
+    tiles = (1 << (end_bit - 32)) - 1 if end_bit < 64 else (1 << 20)
+    keys = random_tile_keys(rng, n, tiles, high_garbage=True, end_bit=end_bit)
+    vals = rng.integers(0, 2**31 - 1, n).astype(np.uint32)
+    cap = max(n, 1)
+    ku = torch.zeros(cap, dtype=torch.int64, device=cuda_device)
+    vu = torch.zeros(cap, dtype=torch.int32, device=cuda_device)
+    ku[:n] = _keys_t(keys, cuda_device)
+    vu[:n] = _t(vals.view(np.int32), cuda_device)
+    ks = torch.full_like(ku, -1)
+    vs = torch.full_like(vu, -1)
+    ws = torch.zeros(ops.get_sort_buffer_size(cap), dtype=torch.int8, device=cuda_device)
+    ops.sort_pairs_bits(n, end_bit, ws, ku, vu, ks, vs)
+    torch.cuda.synchronize()
+    ek, ev = O.sort_pairs(keys, vals, end_bit)
+    np.testing.assert_array_equal(_np_keys(ks)[:n], ek)  # bit-exact keys
+    np.testing.assert_array_equal(_np_vals(vs)[:n], ev)  # stable: values bit-exact too
+    np.testing.assert_array_equal(_np_keys(ku)[:n], keys)  # input preserved
+
+
+def test_sort_gaussian_op_uses_tile_width(cuda_device):
+    rng = np.random.default_rng(7)
+    W, H = 1920, 1080
+    tiles = ((W + 15) // 16) * ((H + 15) // 16)
+    n = 300_000
+    keys = random_tile_keys(rng, n, tiles)
+    vals = rng.permutation(n).astype(np.uint32)
+    ku, vu = _keys_t(keys, cuda_device), _t(vals.view(np.int32), cuda_device)
+    ks, vs = torch.empty_like(ku), torch.empty_like(vu)
+    ws = torch.zeros(ops.get_sort_buffer_size(n), dtype=torch.int8, device=cuda_device)
+    ops.sort_gaussian(n, W, H, 16, 16, ws, ku, vu, ks, vs)
+    ek, ev = O.sort_pairs(keys, vals, O.end_bit_for(W, H))
+    np.testing.assert_array_equal(_np_keys(ks), ek)
+    np.testing.assert_array_equal(_np_vals(vs), ev)
+
+
+def test_sort_device_count_via_c_abi(cuda_device):
+    """Count read from device memory (the no-sync path of the fused forward)."""
+    rng = np.random.default_rng(3)
+    cap, n = 200_000, 123_457
+    keys = random_tile_keys(rng, cap, 8000)
+    vals = np.arange(cap, dtype=np.uint32)
+    ku, vu = _keys_t(keys, cuda_device), _t(vals.view(np.int32), cuda_device)
+    ks, vs = torch.zeros_like(ku), torch.zeros_like(vu)
+    ws = torch.zeros(ops.get_sort_buffer_size(cap), dtype=torch.int8, device=cuda_device)
+    cnt = torch.tensor([n], dtype=torch.int32, device=cuda_device)
+    st = lib().gsr_sort_bits(0, cnt.data_ptr(), 45, ws.data_ptr(), ws.numel(), ku.data_ptr(), vu.data_ptr(),
+                             ks.data_ptr(), vs.data_ptr(), cap, torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    torch.cuda.synchronize()
+    ek, ev = O.sort_pairs(keys[:n], vals[:n], 45)
+    np.testing.assert_array_equal(_np_keys(ks)[:n], ek)
+    np.testing.assert_array_equal(_np_vals(vs)[:n], ev)
+
+
+# ---------------------------------------------------------------------------- ranges / gather
+
+@pytest.mark.parametrize("n,W,H", [(0, 800, 600), (1, 800, 600), (5000, 64, 64), (250_000, 1920, 1080)])
+def test_tile_ranges_bit_exact(cuda_device, n, W, H):
+    rng = np.random.default_rng(n + W)
+    tiles = ((W + 15) // 16) * ((H + 15) // 16)
+    keys = np.sort(random_tile_keys(rng, n, max(1, tiles // 3)) + (np.uint64(tiles // 3) << np.uint64(32)))
+    ks = _keys_t(keys, cuda_device) if n else torch.zeros(1, dtype=torch.int64, device=cuda_device)
+    for scan in (False, True):
+        rb = torch.full((tiles + 5, 2), -7, dtype=torch.int32, device=cuda_device)
+        (ops.precompute_tile_ranges_scan if scan else ops.precompute_tile_ranges)(n, W, H, 16, 16, ks, rb)
+        got = rb.cpu().numpy()
+        np.testing.assert_array_equal(got[:tiles], O.tile_ranges(keys, tiles, scan=scan))
+        assert (got[tiles:] == -7).all()  # nothing written past the tile count
+
+
+def test_gather_bit_exact(cuda_device):
+    rng = np.random.default_rng(5)
+    P, n = 10_000, 77_777
+    xy = rng.standard_normal((P, 2)).astype(np.float32)
+    rgbd = rng.standard_normal((P, 4)).astype(np.float32)
+    con = rng.standard_normal((P, 4)).astype(np.float32)
+    v = rng.integers(0, P, n).astype(np.uint32)
+    dst = [torch.zeros((n, k), dtype=torch.float32, device=cuda_device) for k in (2, 4, 4)]
+    ops.gather_features(n, _t(v.view(np.int32), cuda_device), _t(xy, cuda_device), _t(rgbd, cuda_device),
+                        _t(con, cuda_device), *dst)
+    for d, e in zip(dst, O.gather(v, xy, rgbd, con)):
+        np.testing.assert_array_equal(d.cpu().numpy(), e)
+
+
+# ---------------------------------------------------------------------------- scene / preprocess
+
+def test_scene_prepare_matches_oracle(cuda_device):
+    sc = scenes.scene_clustered(20_000, seed=9)
+    op, cov = ops.prepare_scene(_t(sc.log_scales, cuda_device), _t(sc.quats, cuda_device),
+                                _t(sc.opacity_logits, cuda_device))
+    eo, ec = O.scene_transform(sc.log_scales, sc.quats, sc.opacity_logits)
+    np.testing.assert_allclose(op.cpu().numpy(), eo, rtol=2e-6, atol=1e-7)
+    # fp32 products vs FP64: relative to the covariance's scale
+    scale = np.abs(ec).max(axis=1, keepdims=True)
+    assert (np.abs(cov.cpu().numpy() - ec) <= 2e-5 * scale + 1e-12).all()
+
+
+def test_loadply_roundtrip(cuda_device, tmp_path):
+    sc = scenes.scene_plain_small(3000, seed=21)
+    p = str(tmp_path / "s.ply")
+    scenes.write_ply(p, sc)
+    num, pos, shs, op, cov = ops.loadPly(p)
+    assert num == 3000 and pos.device.type == "cpu"
+    np.testing.assert_array_equal(pos.numpy(), sc.means)
+    np.testing.assert_array_equal(shs.numpy(), sc.shs.reshape(3000, 48))
+    eo, ec = O.scene_transform(sc.log_scales, sc.quats, sc.opacity_logits)
+    np.testing.assert_allclose(op.numpy(), eo, rtol=2e-6, atol=1e-7)
+    scale = np.abs(ec).max(axis=1, keepdims=True)
+    assert (np.abs(cov.numpy() - ec) <= 2e-5 * scale + 1e-12).all()
+
+
+def _gpu_scene(raw, dev):
+    return Scene.from_raw(raw, dev)
+
+
+CASES = {
+    "small_800x600": (lambda: scenes.subsample(scenes.scene_plain_small(), 30_000, seed=1),
+                      lambda: scenes.camera_front(800, 600, 600.0)),
+    "clustered_640x360": (lambda: scenes.subsample(scenes.scene_clustered(600_000, seed=1), 60_000, seed=2),
+                          lambda: scenes.camera_front(640, 360, 1400.0 / 3)),
+    "orbit_1280x720": (lambda: scenes.scene_clustered(50_000, seed=33),
+                       lambda: scenes.orbit_camera(8.0, 0.7, 0.3, 1280, 720, scenes.focal_for(1280))),
+}
+
+
+def _run_preprocess(scene, cam, dev, half):
+    P = scene.num_vertex
+    cap = 4_000_000
+    ku = torch.zeros(cap, dtype=torch.int64, device=dev)
+    vu = torch.zeros(cap, dtype=torch.int32, device=dev)
+    xy = torch.zeros((P, 2), device=dev)
+    rgbd = torch.zeros((P, 4), device=dev)
+    con = torch.zeros((P, 4), device=dev)
+    cnt = torch.zeros(1, dtype=torch.int32, device=dev)
+    c = Camera.from_spec(cam)
+    fn = ops.preprocess_half_sh if half else ops.preprocess
+    fn(scene.position, scene.shs_half if half else scene.shs, scene.opacity, scene.cov3d, c.width, c.height, 16,
+       16, c.position, c.rotation, c.focal_x, c.focal_y, c.zFar, c.zNear, xy, rgbd, con, ku, vu, cnt)
+    n = int(cnt.item())
+    return n, ku[:n], vu[:n], xy, rgbd, con
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("half", [False, True])
+def test_preprocess_vs_oracle(cuda_device, case, half):
+    raw = CASES[case][0]()
+    cam = CASES[case][1]()
+    scene = _gpu_scene(raw, cuda_device)
+    n, ku, vu, xy, rgbd, con = _run_preprocess(scene, cam, cuda_device, half)
+    shs = raw.shs.reshape(-1, 48)
+    if half:
+        shs = shs.astype(np.float16).astype(np.float32)
+    cp, cr = O.camera_args(cam)
+    pre = O.preprocess(raw.means, shs, scene.opacity.cpu().numpy(), scene.cov3d.cpu().numpy(), cam.width,
+                       cam.height, cp, cr, cam.fx, cam.fy)
+    gk, gv = _np_keys(ku), _np_vals(vu)
+    only_g, only_o, ulp = compare_key_lists(gk, gv, pre["keys"], pre["vals"])
+    tol = max(8, int(1e-4 * pre["num"]))
+    assert only_g + only_o <= tol, (n, pre["num"], only_g, only_o)
+    assert ulp <= 2, ulp
+    # features of Gaussians both sides emitted
+    em = pre["emitted"] & np.isin(np.arange(raw.num), gv)
+    for g, e, what in ((xy, pre["xy"], "xy"), (rgbd, pre["rgbd"], "rgbd"), (con, pre["con"], "con")):
+        a, b = g.cpu().numpy()[em], e[em]
+        err = np.abs(a - b) / (np.abs(b) + 1e-3)
+        assert err.max() < 2e-4, (what, err.max())
+
+
+# ---------------------------------------------------------------------------- render / forward
+
+def _oracle_lists_from_gpu(n, ks, vs, W, H):
+    keys, vals = _np_keys(ks)[:n], _np_vals(vs)[:n]
+    tiles = ((W + 15) // 16) * ((H + 15) // 16)
+    return vals, O.tile_ranges(keys, tiles)
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("variant", ["lite", "fused", "default", "dt", "preranges"])
+def test_render_variants_vs_oracle(cuda_device, case, variant):
+    """Same sorted lists and features into the GPU blend and the FP64 blend."""
+    raw, cam = CASES[case][0](), CASES[case][1]()
+    scene = _gpu_scene(raw, cuda_device)
+    n, ku, vu, xy, rgbd, con = _run_preprocess(scene, cam, cuda_device, True)
+    ks, vs = torch.empty_like(ku), torch.empty_like(vu)
+    ws = torch.zeros(ops.get_sort_buffer_size(max(n, 1)), dtype=torch.int8, device=cuda_device)
+    ops.sort_gaussian(n, cam.width, cam.height, 16, 16, ws, ku, vu, ks, vs)
+    W, H = cam.width, cam.height
+    tiles = ((W + 15) // 16) * ((H + 15) // 16)
+    rb = torch.zeros((tiles, 2), dtype=torch.int32, device=cuda_device)
+    ops.precompute_tile_ranges(n, W, H, 16, 16, ks, rb)
+    out = torch.zeros((H, W, 3), dtype=torch.uint8, device=cuda_device)
+    bg = torch.tensor([0.1, 0.3, 0.7])
+    cadence = {"lite": 8, "fused": 16, "default": 2, "dt": 8, "preranges": 2}[variant]
+    if variant == "lite":
+        ops.render_16x16_preranges_smem_persistent_lite(n, W, H, xy, rgbd, con, vs, rb, bg, out)
+    elif variant == "fused":
+        ops.render_16x16_preranges_smem_persistent_lite_fused(n, W, H, xy, rgbd, con, ks, vs, bg, out)
+    elif variant == "default":
+        ops.render_16x16(n, W, H, xy, rgbd, con, ks, vs, bg, out)
+    elif variant == "dt":
+        ops.render_16x16_preranges_smem_persistent_lite_dt(n, W, H, xy, rgbd, con, vs, rb, bg, out)
+    else:
+        ops.render_16x16_preranges(n, W, H, xy, rgbd, con, vs, rb, bg, out)
+    vals, rng = _oracle_lists_from_gpu(n, ks, vs, W, H)
+    np.testing.assert_array_equal(rb.cpu().numpy(), rng)
+    exp = O.render(vals, rng, xy.cpu().numpy(), rgbd.cpu().numpy(), con.cpu().numpy(), W, H, bg.numpy(),
+                   cadence=cadence, dt=(variant == "dt"))
+    s = image_stats(out.cpu().numpy(), exp)
+    assert s["max_abs"] <= 2 and s["psnr"] >= 50.0, s
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("variant", ["e2e", "e2e_preranges", "default"])
+def test_forward_vs_fp64_oracle(cuda_device, case, variant):
+    """Whole frame through the fused entry points against the FP64 oracle."""
+    raw, cam = CASES[case][0](), CASES[case][1]()
+    scene = _gpu_scene(raw, cuda_device)
+    rast = Rasterizer(scene, 4_000_000, 1 << 16)
+    c = Camera.from_spec(cam)
+    bg = torch.zeros(3)
+    name = {"e2e": "preranges_smem_persistent_lite_e2e", "e2e_preranges": "preranges_smem_persistent_lite_e2e_preranges",
+            "default": "default"}[variant]
+    img, st = rast.forward(scene, c, bg, render_variant=name, return_stats=True)
+    half = variant != "default"
+    cadence = {"e2e": 16, "e2e_preranges": 8, "default": 2}[variant]
+    exp, pre = O.forward(raw.means, raw.shs, scene.opacity.cpu().numpy(), scene.cov3d.cpu().numpy(), cam,
+                         cadence=cadence, half_sh=half)
+    assert abs(st["num_rendered"] - pre["num"]) <= max(8, int(1e-4 * pre["num"]))
+    s = image_stats(img.cpu().numpy(), exp)
+    assert s["max_abs"] <= 2 and s["psnr"] >= 50.0, s
+
+
+def test_overflow_reports_true_count(cuda_device):
+    raw, cam = CASES["small_800x600"][0](), CASES["small_800x600"][1]()
+    scene = _gpu_scene(raw, cuda_device)
+    rast = Rasterizer(scene, 1000, 1 << 16)
+    with pytest.raises(GsrError) as ei:
+        rast.forward(scene, Camera.from_spec(cam), torch.zeros(3), render_variant="preranges_smem_persistent_lite_e2e")
+    assert ei.value.status == 1 and ei.value.num > 1000
+    # the context is still usable: a big enough rasterizer renders the frame
+    rast2 = Rasterizer(scene, 2_000_000, 1 << 16)
+    rast2.forward(scene, Camera.from_spec(cam), torch.zeros(3), render_variant="preranges_smem_persistent_lite_e2e")
+    torch.cuda.synchronize()
+
+
+def test_rasterizer_stage_timings_and_variants_agree(cuda_device):
+    raw, cam = CASES["clustered_640x360"][0](), CASES["clustered_640x360"][1]()
+    scene = _gpu_scene(raw, cuda_device)
+    rast = Rasterizer(scene, 4_000_000, 1 << 16)
+    c = Camera.from_spec(cam)
+    bg = torch.zeros(3)
+    a = rast.forward(scene, c, bg, render_variant="preranges_smem_persistent_lite_e2e").clone()
+    out, pre, srt, ren = rast.forward(scene, c, bg, render_variant="preranges_smem_persistent_lite",
+                                      measure_preprocess=True, measure_sort=True, measure_render=True)
+    assert pre > 0 and srt > 0 and ren > 0
+    s = image_stats(a.cpu().numpy(), out.cpu().numpy())
+    assert s["max_abs"] <= 2 and s["psnr"] >= 50.0, s
+    _, st = rast.forward(scene, c, bg, return_stats=True)
+    assert st["render_variant"] == "default" and st["num_rendered"] > 0
