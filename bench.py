@@ -1,0 +1,374 @@
+"""Benchmark of the GB300 3DGS forward path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl gsr|reference]
+
+A step is one frame of the plain forward (preprocess -> tile-key radix sort
+-> tile ranges -> persistent blend) over a resident seeded synthetic scene.
+Default workload: ``plain_3m_1080p`` (3,000,000 Gaussians, clustered with a
+heavy-tailed scale distribution, 1920x1080, fx=fy=1400, 16x16 tiles, FP16
+SH -- the reference's E2E variant ``preranges_smem_persistent_lite_e2e``).
+
+value     frames/s, device-timed over K back-to-back frames (CUDA events on
+          the launching stream; inputs resident in HBM; the scene, 408 MB,
+          is larger than L2, so no flush is needed between frames).
+e2e       frames/s through the public drop-in API (Rasterizer.forward with
+          the host-read camera/background, status read-back and the frame
+          copied to pinned host memory every step).
+roofline  the dominant kernel of the frame, timed live with CUDA events
+          recorded between stages on the launching stream.
+cpu_baseline  the FP64 CPU oracle (oracle/), multithreaded, on whole frames.
+
+--impl reference runs the reference's CPU arm: the reference ships no CPU
+path, so this is the FP64 oracle restatement of its algorithm on all host
+cores.  Multi-GPU: replicas only (one independent renderer per rank).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+E2E_VARIANT = "preranges_smem_persistent_lite_e2e"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", default="plain_3m_1080p")
+    ap.add_argument("--impl", default="gsr", choices=["gsr", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- peaks
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def committed_traffic(workload: str, kernel: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(workload, {}).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+# ----------------------------------------------------------------------------- CPU arm
+def cpu_frames(raw, cam, seconds: float, half: bool = True):
+    """Time the FP64 oracle on whole frames for about `seconds`."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    op, cov = O.scene_transform(raw.log_scales, raw.quats, raw.opacity_logits)
+    threads = O.nthreads_default()
+    n, t0 = 0, time.perf_counter()
+    while True:
+        O.forward(raw.means, raw.shs, op, cov, cam, cadence=16, half_sh=half, nthreads=threads)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 50:
+            break
+    return n / el, threads, n, el
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from polysplat_gb300 import scenes
+
+    raw, cams = scenes.workload(args.workload)
+    cam = cams[0]
+    from oracle import oracle as O
+
+    op, cov = O.scene_transform(raw.log_scales, raw.quats, raw.opacity_logits)
+    threads = O.nthreads_default()
+    for _ in range(max(0, min(args.warmup, 1))):
+        O.forward(raw.means, raw.shs, op, cov, cam, cadence=16, half_sh=True, nthreads=threads)
+    steps = max(1, min(args.steps, 8))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        O.forward(raw.means, raw.shs, op, cov, cam, cadence=16, half_sh=True, nthreads=threads)
+    el = time.perf_counter() - t0
+    fps = steps / el
+    line = {"impl": "reference", "metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1000.0 * el / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "width": cam.width, "height": cam.height,
+                       "gaussians": raw.num, "variant": E2E_VARIANT},
+            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
+                             "sample": "%d whole frames of %s (FP64 oracle restatement; the reference ships no "
+                                       "CPU render path)" % (steps, args.workload)},
+            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def run_gsr(args):
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist = dist_mod
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from polysplat_gb300 import Camera, Rasterizer, Scene, ops, scenes
+    from polysplat_gb300._lib import check, lib
+
+    raw, cams = scenes.workload(args.workload)
+    cam_spec = cams[0]
+    scene = Scene.from_raw(raw, dev)
+    cam = Camera.from_spec(cam_spec)
+    cap = 1 << 28 if raw.num > 10_000_000 else 1 << 26
+    rast = Rasterizer(scene, cap, 1 << 18)
+    bg = torch.zeros(3)
+
+    # ---- device-timed value: the fused forward through the C ABI (no host sync per frame)
+    L = lib()
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    cam_pos = (ctypes.c_float * 3)(*cam.position.tolist())
+    cam_rot = (ctypes.c_float * 9)(*cam.rotation.reshape(-1).tolist())
+    bgc = (ctypes.c_float * 3)(0.0, 0.0, 0.0)
+    out = torch.zeros((cam.height, cam.width, 3), dtype=torch.uint8, device=dev)
+    ws = rast.list_sorting_space
+    wsb = ws.numel()
+
+    def frame():
+        st = L.gsr_forward(1, scene.num_vertex, scene.position.data_ptr(), scene.shs_half.data_ptr(), 1,
+                           scene.opacity.data_ptr(), scene.cov3d.data_ptr(), cam.width, cam.height, 16, 16, cam_pos,
+                           cam_rot, cam.focal_x, cam.focal_y, cam.zFar, cam.zNear, rast.curr_offset.data_ptr(),
+                           ws.data_ptr(), wsb, rast.gaussian_keys_unsorted.data_ptr(),
+                           rast.gaussian_values_unsorted.data_ptr(), rast.gaussian_keys_sorted.data_ptr(),
+                           rast.gaussian_values_sorted.data_ptr(), cap, rast.points_xy.data_ptr(),
+                           rast.rgb_depth.data_ptr(), rast.conic_opacity.data_ptr(), None, bgc, out.data_ptr(), sh)
+        check(st, "forward")
+
+    for _ in range(max(3, args.warmup)):
+        frame()
+    num = ops._read_status(ws, rast.curr_offset, cap, "forward")
+    tiles = ((cam.width + 15) // 16) * ((cam.height + 15) // 16)
+    end_bit = 32 + tiles.bit_length()
+    passes = (end_bit + 7) // 8
+
+    # stage events recorded by the library: [preprocess, upsweep, pass 0..passes-1, render]
+    K = args.steps
+    check(L.gsr_profile_begin(K), "profile_begin")
+
+    sampler = ClockSampler(local)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(K):
+        frame()
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    MAXS = 16
+    ms_buf = (ctypes.c_float * (K * MAXS))()
+    n_stages = L.gsr_profile_read(ms_buf, K, MAXS)
+    L.gsr_profile_end()
+    if dist is not None:
+        dist.barrier()
+    clocks = sampler.stop()
+    elapsed_ms = t_start.elapsed_time(t_end)
+    if dist is not None:
+        t = torch.tensor([elapsed_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    fps = world * K / (elapsed_ms / 1000.0)
+
+    stage_names = ["preprocess", "sort_upsweep"] + ["sort_pass%d" % p for p in range(passes)] + ["render"]
+    if n_stages != len(stage_names):
+        raise RuntimeError("expected %d timed stages, the library recorded %d" % (len(stage_names), n_stages))
+    stage_avg = {nm: statistics.mean(ms_buf[f * MAXS + i] for f in range(K)) for i, nm in enumerate(stage_names)}
+    pass_avg = statistics.mean([stage_avg["sort_pass%d" % p] for p in range(passes)])
+
+    # algorithmic bytes per launch (formulas in the design doc)
+    P = scene.num_vertex
+    peak, peak_kind = measured_peaks()
+    pass_bytes = 24.0 * num  # read key+value, write key+value
+    pre_bytes = P * (12 + 4 + 24 + 96) + num * 12
+    cand = {"k_pass": (pass_avg, pass_bytes), "k_preprocess": (stage_avg["preprocess"], pre_bytes)}
+    dom = max(cand, key=lambda k: cand[k][0] * (passes if k == "k_pass" else 1))
+    dur_ms, abytes = cand[dom]
+    achieved = abytes / (dur_ms / 1000.0) / 1e9
+    traffic = committed_traffic(args.workload, dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                "algorithmic_bytes": abytes, "avg_launch_ms": dur_ms}
+
+    # ---- e2e through the public API
+    host = torch.empty((cam.height, cam.width, 3), dtype=torch.uint8, pin_memory=True)
+    for _ in range(2):
+        img = rast.forward(scene, cam, bg, render_variant=E2E_VARIANT)
+        host.copy_(img, non_blocking=True)
+    torch.cuda.synchronize()
+    Ke = max(5, K // 2)
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        img = rast.forward(scene, cam, bg, render_variant=E2E_VARIANT)
+        host.copy_(img, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_fps = world * Ke / e2e_s
+
+    # ---- the reference's own GPU pipeline on this GB300 (its kernels + its CUB sort call)
+    ref_gpu = None
+    try:
+        from oracle import refkernels as RK
+
+        if RK.available() and world == 1:
+            # the reference writes keys unchecked: size its buffers from this
+            # library's (capacity-safe) count with a wide margin
+            cap_ref = max(1 << 20, 2 * num)
+            pipe = RK.Pipeline(scene, cam_spec, cap_ref)
+            for _ in range(3):
+                pipe.forward()
+            torch.cuda.synchronize()
+            ts = []
+            for _ in range(K):
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record()
+                n_ref = pipe.forward()
+                b.record()
+                b.synchronize()
+                ts.append(a.elapsed_time(b))
+            ref_ms = statistics.mean(ts)
+            ref_img_equal = bool(torch.equal(pipe.out, rast.forward(scene, cam, bg, render_variant=E2E_VARIANT)))
+            ref_gpu = {"value": 1000.0 / ref_ms, "unit": "frames/s", "ms_per_frame": ref_ms,
+                       "median_ms": statistics.median(ts), "num_rendered": n_ref, "image_identical": ref_img_equal,
+                       "what": "reference preprocess/render kernels built from its sources + its CUB SortPairs "
+                               "call, E2E sequence of forward_fused_e2e incl. its per-frame count read-back"}
+            del pipe
+            torch.cuda.empty_cache()
+    except Exception as exc:  # the comparison is informative, not required
+        ref_gpu = {"unavailable": str(exc)[:200]}
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            cfps, threads, n, el = cpu_frames(raw, cam_spec, seconds=15.0)
+            cpu = {"value": cfps, "unit": "frames/s", "cores": threads, "kind": "port",
+                   "sample": "%d whole frames of %s in %.1f s (FP64 oracle, %d threads)" % (n, args.workload, el,
+                                                                                          threads)}
+        launches_per_frame = 1 + 1 + passes + 1
+        line = {"metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": world, "steps": K,
+                "warmup": max(3, args.warmup), "ms_per_step": elapsed_ms / K, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": args.workload, "gaussians": P, "width": cam.width, "height": cam.height,
+                           "tile": "16x16", "variant": E2E_VARIANT, "sh": "fp16", "num_rendered": num,
+                           "sort_bits": end_bit, "l2": "inputs larger than L2 (scene %.0f MB)" %
+                           (scene.device_bytes() / 1e6), "parallelism": "replicas" if world > 1 else "single"},
+                "stages_ms": stage_avg, "roofline": roofline, "cpu_baseline": cpu, "reference_gpu": ref_gpu,
+                "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": 60,
+                        "d2h_bytes_per_step": cam.width * cam.height * 3 + 4},
+                "gpu_launches": launches_per_frame * K, "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gsr(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -62,7 +62,8 @@ gsr_status gsr_device_check(int device);
  * (csrc/cuda_rasterizer/sort.cu:127-149, csrc/pybind.cpp:346-349); the
  * workspace is the reference's `list_sorting_space`. */
 size_t gsr_workspace_size(int64_t capacity);
-/* Small workspace (status word + tile queue) for render-only calls. */
+/* Small workspace (status word, render tile queue, large-Gaussian queue) for
+ * preprocess-only and render-only calls. */
 size_t gsr_render_workspace_size(void);
 /* Clear the workspace's status word (asynchronous). */
 gsr_status gsr_workspace_reset(void* workspace, gsr_stream_t stream);
@@ -71,6 +72,12 @@ gsr_status gsr_workspace_reset(void* workspace, gsr_stream_t stream);
  * capacity, in which case GSR_OVERFLOW is returned). */
 gsr_status gsr_read_status(const void* workspace, const int32_t* d_num, int64_t capacity, int32_t* num_out,
                            gsr_stream_t stream);
+
+/* View and projection matrices (column-major float[16]) the preprocess uses
+ * for a camera; host-side, no GPU work.  Replaces getViewMatrix /
+ * getProjectionMatrix (csrc/cuda_rasterizer/preprocess.cu:643-671). */
+void gsr_camera_matrices(int width, int height, const float* cam_pos, const float* cam_rot, float focal_x,
+                         float focal_y, float z_far, float z_near, float* view16, float* proj16);
 
 /* ---- scene preparation -------------------------------------------------- */
 /* Raw INRIA parameters -> render inputs: opacity = sigmoid(logit),
@@ -84,13 +91,18 @@ gsr_status gsr_scene_prepare(int P, const float* log_scales, const float* quats,
 /* Projection, EWA conic, degree-3 SH colour, culling and tile-key emission.
  * Keys are appended at *curr_offset (atomically); writes past
  * key_capacity are dropped but counted.  shs_half != 0 selects FP16 SH.
- * Replaces preprocess / preprocess_half_sh (csrc/ops.h:42-48, 104-111;
- * csrc/cuda_rasterizer/preprocess.cu:1252-1330; csrc/pybind.cpp:122-181). */
+ * `workspace` (at least gsr_render_workspace_size() bytes, or NULL) holds
+ * the queue of Gaussians with large tile rectangles, which a second kernel
+ * spreads over whole CTAs; without it those are emitted by their own warp
+ * (same keys, slower).  Replaces preprocess / preprocess_half_sh
+ * (csrc/ops.h:42-48, 104-111; csrc/cuda_rasterizer/preprocess.cu:1252-1330;
+ * csrc/pybind.cpp:122-181). */
 gsr_status gsr_preprocess(int P, const float* pos, const void* shs, int shs_half, const float* opacity,
                           const float* cov3d, int width, int height, int block_x, int block_y,
                           const float* cam_pos, const float* cam_rot, float focal_x, float focal_y, float z_far,
                           float z_near, float* points_xy, float* rgb_depth, float* conic_opacity, uint64_t* keys,
-                          uint32_t* values, int64_t key_capacity, int32_t* curr_offset, gsr_stream_t stream);
+                          uint32_t* values, int64_t key_capacity, int32_t* curr_offset, void* workspace,
+                          size_t workspace_bytes, gsr_stream_t stream);
 
 /* ---- sort ----------------------------------------------------------------- */
 /* Stable ascending LSD radix sort of (u64 key, u32 value) pairs over bits
@@ -149,6 +161,22 @@ gsr_status gsr_forward(int variant, int P, const float* pos, const void* shs, in
                        uint32_t* values_unsorted, uint64_t* keys_sorted, uint32_t* values_sorted,
                        int64_t key_capacity, float* points_xy, float* rgb_depth, float* conic_opacity,
                        int32_t* ranges, const float* bg_color, uint8_t* out_color, gsr_stream_t stream);
+
+/* ---- stage timing ------------------------------------------------------- */
+/* Profiling hook with no counterpart in the reference.  After
+ * gsr_profile_begin(frames), each of the next `frames` gsr_forward calls
+ * records library-owned CUDA events on its stream before the preprocess and
+ * after every stage (preprocess, sort upsweep, each radix pass, tile ranges
+ * when the variant needs them, render).  gsr_profile_read() synchronises and
+ * writes the stage durations in ms, row f = frame f, `max_stages` columns,
+ * and returns the number of stages per frame (or -1).  gsr_profile_end()
+ * stops recording and frees the events. */
+gsr_status gsr_profile_begin(int frames);
+int gsr_profile_read(float* ms, int frames, int max_stages);
+void gsr_profile_end(void);
+
+/* Text of the last CUDA error seen by the library (for diagnostics). */
+const char* gsr_last_error(void);
 
 #ifdef __cplusplus
 }

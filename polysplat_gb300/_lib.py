@@ -32,6 +32,8 @@ class GsrError(RuntimeError):
         msg = "gsr %s failed: %s" % (where, STATUS_NAMES.get(status, str(status)))
         if status == GSR_OVERFLOW:
             msg += " (%d keys emitted; the key buffers are too small)" % num
+        if status == GSR_CUDA_ERROR and _lib is not None:
+            msg += " (%s)" % _lib.gsr_last_error().decode(errors="replace")
         super().__init__(msg)
 
 
@@ -46,7 +48,7 @@ def _declare(L):
         "gsr_read_status": ([P, P, i64, P, P], i32),
         "gsr_scene_prepare": ([i32, P, P, P, P, P, P], i32),
         "gsr_preprocess": ([i32, P, P, i32, P, P, i32, i32, i32, i32, P, P, f32, f32, f32, f32,
-                            P, P, P, P, P, i64, P, P], i32),
+                            P, P, P, P, P, i64, P, P, sz, P], i32),
         "gsr_sort": ([i32, P, i32, i32, i32, i32, P, sz, P, P, P, P, i64, P], i32),
         "gsr_sort_bits": ([i32, P, i32, P, sz, P, P, P, P, i64, P], i32),
         "gsr_tile_ranges": ([i32, P, i32, i32, i32, i32, P, P, i32, P], i32),
@@ -55,6 +57,11 @@ def _declare(L):
         "gsr_forward": ([i32, i32, P, P, i32, P, P, i32, i32, i32, i32, P, P, f32, f32, f32, f32,
                          P, P, sz, P, P, P, P, i64, P, P, P, P, P, P, P], i32),
     }
+    sig["gsr_camera_matrices"] = ([i32, i32, P, P, f32, f32, f32, f32, P, P], None)
+    sig["gsr_profile_begin"] = ([i32], i32)
+    sig["gsr_profile_read"] = ([P, i32, i32], i32)
+    sig["gsr_profile_end"] = ([], None)
+    sig["gsr_last_error"] = ([], ctypes.c_char_p)
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
         fn.argtypes = args

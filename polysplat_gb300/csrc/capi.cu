@@ -19,9 +19,34 @@ int device_sm_count()
     return cached[dev];
 }
 
+// Stage-timing state: `frames` rows of kMarks events; row g_prof_row is the
+// one the current forward records into.
+constexpr int kMarks = 16;
+static cudaEvent_t* g_prof = nullptr;
+static int g_prof_frames = 0;
+static int g_prof_row = -1;
+static int g_prof_mark = 0;
+static int g_prof_marks_per_frame = 0;
+static cudaError_t g_last_error = cudaSuccess;
+
+void profile_mark(cudaStream_t stream)
+{
+    if (!g_prof || g_prof_row < 0 || g_prof_row >= g_prof_frames || g_prof_mark >= kMarks) return;
+    cudaEventRecord(g_prof[g_prof_row * kMarks + g_prof_mark++], stream);
+}
+
+static void profile_frame_begin()
+{
+    if (!g_prof) return;
+    if (g_prof_row >= 0 && g_prof_mark > 0) g_prof_marks_per_frame = g_prof_mark;
+    g_prof_row++;
+    g_prof_mark = 0;
+}
+
 static gsr_status from_cuda(cudaError_t e)
 {
     if (e == cudaSuccess) return GSR_OK;
+    g_last_error = e;
     if (e == cudaErrorInvalidValue) return GSR_INVALID_ARG;
     return GSR_CUDA_ERROR;
 }
@@ -47,6 +72,56 @@ extern "C" {
 
 int gsr_version(void) { return 1; }
 
+void gsr_profile_end(void)
+{
+    if (g_prof) {
+        for (int i = 0; i < g_prof_frames * kMarks; i++)
+            if (g_prof[i]) cudaEventDestroy(g_prof[i]);
+        delete[] g_prof;
+    }
+    g_prof = nullptr;
+    g_prof_frames = 0;
+    g_prof_row = -1;
+    g_prof_mark = 0;
+    g_prof_marks_per_frame = 0;
+}
+
+gsr_status gsr_profile_begin(int frames)
+{
+    gsr_profile_end();
+    if (frames <= 0) return GSR_INVALID_ARG;
+    g_prof = new cudaEvent_t[(size_t)frames * kMarks]();
+    g_prof_frames = frames;
+    for (int i = 0; i < frames * kMarks; i++) {
+        cudaError_t e = cudaEventCreate(&g_prof[i]);
+        if (e != cudaSuccess) {
+            gsr_profile_end();
+            return from_cuda(e);
+        }
+    }
+    return GSR_OK;
+}
+
+int gsr_profile_read(float* ms, int frames, int max_stages)
+{
+    if (!g_prof || !ms) return -1;
+    if (g_prof_row >= 0 && g_prof_mark > 0) g_prof_marks_per_frame = g_prof_mark;
+    const int stages = g_prof_marks_per_frame - 1;
+    if (stages <= 0) return -1;
+    const int rows = g_prof_row + 1 < frames ? g_prof_row + 1 : frames;
+    for (int f = 0; f < rows && f < g_prof_frames; f++) {
+        if (cudaEventSynchronize(g_prof[f * kMarks + stages]) != cudaSuccess) return -1;
+        for (int k = 0; k < stages && k < max_stages; k++) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, g_prof[f * kMarks + k], g_prof[f * kMarks + k + 1]);
+            ms[f * max_stages + k] = t;
+        }
+    }
+    return stages;
+}
+
+const char* gsr_last_error(void) { return cudaGetErrorString(g_last_error); }
+
 gsr_status gsr_device_check(int device)
 {
     cudaDeviceProp prop;
@@ -57,7 +132,7 @@ gsr_status gsr_device_check(int device)
 
 size_t gsr_workspace_size(int64_t capacity) { return sort_workspace_bytes(capacity); }
 
-size_t gsr_render_workspace_size(void) { return kHeaderBytes; }
+size_t gsr_render_workspace_size(void) { return kSmallWorkspaceBytes; }
 
 gsr_status gsr_workspace_reset(void* workspace, gsr_stream_t stream)
 {
@@ -84,6 +159,12 @@ gsr_status gsr_read_status(const void* workspace, const int32_t* d_num, int64_t 
     return GSR_OK;
 }
 
+void gsr_camera_matrices(int width, int height, const float* cam_pos, const float* cam_rot, float focal_x,
+                         float focal_y, float z_far, float z_near, float* view16, float* proj16)
+{
+    camera_matrices(width, height, cam_pos, cam_rot, focal_x, focal_y, z_far, z_near, view16, proj16);
+}
+
 gsr_status gsr_scene_prepare(int P, const float* log_scales, const float* quats, const float* opacity_logits,
                              float* opacity, float* cov3d, gsr_stream_t stream)
 {
@@ -96,7 +177,7 @@ static gsr_status preprocess_impl(int P, const float* pos, const void* shs, int 
                                   const float* cam_pos, const float* cam_rot, float fx, float fy, float zfar,
                                   float znear, float* points_xy, float* rgb_depth, float* conic_opacity,
                                   uint64_t* keys, uint32_t* values, int64_t cap, int32_t* curr_offset,
-                                  cudaStream_t s)
+                                  void* workspace, size_t workspace_bytes, cudaStream_t s)
 {
     if (P < 0 || width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0 || !cam_pos || !cam_rot || !curr_offset)
         return GSR_INVALID_ARG;
@@ -130,6 +211,16 @@ static gsr_status preprocess_impl(int P, const float* pos, const void* shs, int 
     p.vals = values;
     p.cap = cap;
     p.counter = curr_offset;
+    p.mq.capacity = 0;
+    p.mq.entries = nullptr;
+    p.mq.count = p.mq.head = nullptr;
+    if (workspace && workspace_bytes >= kSmallWorkspaceBytes) {
+        WorkspaceHeader* h = reinterpret_cast<WorkspaceHeader*>(workspace);
+        p.mq.entries = reinterpret_cast<MassiveEntry*>(reinterpret_cast<char*>(workspace) + kHeaderBytes);
+        p.mq.capacity = kMassiveQueueEntries;
+        p.mq.count = &h->mq_count;
+        p.mq.head = &h->mq_head;
+    }
     return from_cuda(launch_preprocess(p, shs_half != 0, s));
 }
 
@@ -137,11 +228,12 @@ gsr_status gsr_preprocess(int P, const float* pos, const void* shs, int shs_half
                           const float* cov3d, int width, int height, int block_x, int block_y, const float* cam_pos,
                           const float* cam_rot, float focal_x, float focal_y, float z_far, float z_near,
                           float* points_xy, float* rgb_depth, float* conic_opacity, uint64_t* keys, uint32_t* values,
-                          int64_t key_capacity, int32_t* curr_offset, gsr_stream_t stream)
+                          int64_t key_capacity, int32_t* curr_offset, void* workspace, size_t workspace_bytes,
+                          gsr_stream_t stream)
 {
     return preprocess_impl(P, pos, shs, shs_half, opacity, cov3d, width, height, block_x, block_y, cam_pos, cam_rot,
                            focal_x, focal_y, z_far, z_near, points_xy, rgb_depth, conic_opacity, keys, values,
-                           key_capacity, curr_offset, (cudaStream_t)stream);
+                           key_capacity, curr_offset, workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
 gsr_status gsr_sort_bits(int num, const int32_t* d_num, int end_bit, void* workspace, size_t workspace_bytes,
@@ -256,13 +348,17 @@ gsr_status gsr_forward(int variant, int P, const float* pos, const void* shs, in
     if (!workspace || !curr_offset || !valid_tile_shape(block_x, block_y)) return GSR_INVALID_ARG;
     if (render_needs_ranges(variant) && !ranges) return GSR_INVALID_ARG;
     if (workspace_bytes < sort_workspace_bytes(key_capacity)) return GSR_INVALID_ARG;
+    profile_frame_begin();
     cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(uint32_t), s);  // status word
     if (e == cudaSuccess) e = cudaMemsetAsync(curr_offset, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return from_cuda(e);
+    profile_mark(s);
     gsr_status st = preprocess_impl(P, pos, shs, shs_half, opacity, cov3d, width, height, block_x, block_y, cam_pos,
                                     cam_rot, focal_x, focal_y, z_far, z_near, points_xy, rgb_depth, conic_opacity,
-                                    keys_unsorted, values_unsorted, key_capacity, curr_offset, s);
+                                    keys_unsorted, values_unsorted, key_capacity, curr_offset, workspace,
+                                    workspace_bytes, s);
     if (st != GSR_OK) return st;
+    profile_mark(s);
     const int tiles = tiles_of(width, height, block_x, block_y);
     st = gsr_sort_bits(0, curr_offset, 32 + bits_for((uint32_t)tiles), workspace, workspace_bytes, keys_unsorted,
                        values_unsorted, keys_sorted, values_sorted, key_capacity, stream);
@@ -270,10 +366,12 @@ gsr_status gsr_forward(int variant, int P, const float* pos, const void* shs, in
     if (render_needs_ranges(variant)) {
         e = launch_tile_ranges(0, curr_offset, key_capacity, tiles, keys_sorted, ranges, false, s);
         if (e != cudaSuccess) return from_cuda(e);
+        profile_mark(s);
     }
-    return render_impl(variant, 0, curr_offset, key_capacity, width, height, block_x, block_y, P, points_xy,
-                       rgb_depth, conic_opacity, keys_sorted, values_sorted, ranges, bg_color, out_color, workspace,
-                       s);
+    st = render_impl(variant, 0, curr_offset, key_capacity, width, height, block_x, block_y, P, points_xy, rgb_depth,
+                     conic_opacity, keys_sorted, values_sorted, ranges, bg_color, out_color, workspace, s);
+    if (st == GSR_OK) profile_mark(s);
+    return st;
 }
 
 }  // extern "C"

@@ -5,7 +5,23 @@
 
 namespace gsr {
 
+// A Gaussian whose tile rectangle is large; its tiles are tested by a whole
+// CTA in the second emission kernel.
+struct MassiveEntry {
+    float4 ctr_power_depth;  // centre x, centre y, power, depth (bits are the key's low word)
+    float4 conic_gid;        // conic x, y, z, Gaussian index (bit pattern)
+    int4 rect;               // tile rectangle [x0, x1) x [y0, y1)
+};
+
+struct MassiveQueue {
+    MassiveEntry* entries;
+    int capacity;
+    uint32_t* count;  // entries pushed (may exceed capacity: the rest were handled in place)
+    uint32_t* head;   // entries taken by the second kernel
+};
+
 struct PreprocessParams {
+    MassiveQueue mq;
     int P;
     const float* pos;
     const void* shs;
@@ -39,11 +55,21 @@ struct WorkspaceHeader {
     uint32_t status;          // OR of kErr* bits
     uint32_t render_queue;    // persistent render tile counter
     uint32_t pass_counter[8]; // per radix pass tile counter
-    uint32_t pad[6];
+    uint32_t mq_count;        // massive-Gaussian queue: entries pushed
+    uint32_t mq_head;         // massive-Gaussian queue: entries taken
+    uint32_t pad[4];
     uint32_t hist[8][256];    // per-pass digit histograms
 };
 constexpr size_t kHeaderBytes = 16384;
 static_assert(sizeof(WorkspaceHeader) <= kHeaderBytes, "header too large");
+
+// Massive-Gaussian queue capacity of a workspace (entries of 48 bytes); the
+// queue sits right after the header.  Gaussians beyond it are emitted in
+// place by their own warp (slower, same keys).
+constexpr int kMassiveQueueEntries = 1 << 18;
+constexpr size_t kMassiveQueueBytes = (size_t)kMassiveQueueEntries * sizeof(MassiveEntry);
+// Small workspace for preprocess-only and render-only calls.
+constexpr size_t kSmallWorkspaceBytes = kHeaderBytes + kMassiveQueueBytes;
 
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;
@@ -92,5 +118,9 @@ struct RenderArgs {
 cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream);
 
 int device_sm_count();
+
+// Stage-timing hook (gsr_set_profile_events): records the next caller-owned
+// event on `stream` when profiling is on; no-op otherwise.
+void profile_mark(cudaStream_t stream);
 
 }  // namespace gsr

@@ -264,11 +264,39 @@ __device__ __forceinline__ void stage_emit(Stage& s, const EmitOut& o, bool vali
     s.fill += n;
 }
 
-__device__ __forceinline__ int warp_max(int v)
+// Tile rectangles at least this large are queued for k_emit_massive.
+constexpr int kMassiveArea = 32;
+
+// Block-wide final flush of every warp's staged keys with one atomic per CTA.
+__device__ __forceinline__ void block_flush(Stage& st, const EmitOut& out, int* s_fill, long long* s_base,
+                                            unsigned lane, int warp)
 {
+    if (lane == 0) s_fill[warp] = st.fill;
+    __syncthreads();
+    if (warp == 0) {
+        int f = lane < kWarps ? s_fill[lane] : 0;
+        int incl = f;
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) v = max(v, __shfl_xor_sync(GSR_FULL_MASK, v, d));
-    return v;
+        for (int d = 1; d < 32; d <<= 1) {
+            int n = __shfl_up_sync(GSR_FULL_MASK, incl, d);
+            if ((int)lane >= d) incl += n;
+        }
+        int total = __shfl_sync(GSR_FULL_MASK, incl, 31);
+        long long base = 0;
+        if (lane == 0 && total > 0) base = atomicAdd(out.counter, total);
+        base = __shfl_sync(GSR_FULL_MASK, base, 0);
+        if (lane < kWarps) s_base[lane] = base + incl - f;
+    }
+    __syncthreads();
+    const long long wb = s_base[warp];
+    for (int i = lane; i < st.fill; i += 32) {
+        long long pos = wb + i;
+        if (pos < out.cap) {
+            out.keys[pos] = st.k[i];
+            out.vals[pos] = st.v[i];
+        }
+    }
+    st.fill = 0;
 }
 
 template <bool HALF>
@@ -347,40 +375,64 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
     }
     point_valid = point_valid && !single;
 
-    // (2) multi-tile Gaussians: massive (whole warp per Gaussian over an 8x4
-    // tile window) or fragmented (flattened task pool), chosen per warp as in
-    // preprocess.cu:439-444.
+    // (2) multi-tile Gaussians.  Rectangles of at least kMassiveArea tiles go
+    // to the massive queue, where a whole CTA tests them (k_emit_massive);
+    // the rest form one flattened task pool per warp (the reference's
+    // "fragmented" scheme, preprocess.cu:521-623).  If the queue is full, the
+    // warp tests the Gaussian itself over an 8x4 tile window (the reference's
+    // "massive" scheme, preprocess.cu:444-519).  Every scheme tests every
+    // tile of the rectangle with the same test, so the key set is the same.
+    bool massive = point_valid && area >= kMassiveArea;
+    {
+        const unsigned mm = __ballot_sync(GSR_FULL_MASK, massive);
+        int qbase = 0;
+        if (mm) {
+            if (lane == 0) qbase = (int)atomicAdd(a.mq.count, (uint32_t)__popc(mm));
+            qbase = __shfl_sync(GSR_FULL_MASK, qbase, 0);
+        }
+        if (massive) {
+            const int slot = qbase + __popc(mm & lanemask_lt());
+            if (slot < a.mq.capacity) {
+                MassiveEntry e;
+                e.ctr_power_depth = make_float4(point_xy.x, point_xy.y, power, p_view.z);
+                e.conic_gid = make_float4(conic.x, conic.y, conic.z, __uint_as_float((uint32_t)idx));
+                e.rect = make_int4(rect_min.x, rect_max.x, rect_min.y, rect_max.y);
+                a.mq.entries[slot] = e;
+                atomicOr(&s_hit[warp], 1u << lane);  // features are written for queued Gaussians
+                point_valid = false;
+                massive = false;
+            }
+        }
+    }
+    // queue overflow: the warp runs the Gaussian's whole rectangle itself
+    unsigned todo = __ballot_sync(GSR_FULL_MASK, massive);
+    while (todo) {
+        const int i = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const float2 c = {__shfl_sync(GSR_FULL_MASK, point_xy.x, i), __shfl_sync(GSR_FULL_MASK, point_xy.y, i)};
+        const float3 q = {__shfl_sync(GSR_FULL_MASK, conic.x, i), __shfl_sync(GSR_FULL_MASK, conic.y, i),
+                          __shfl_sync(GSR_FULL_MASK, conic.z, i)};
+        const int x_lo = __shfl_sync(GSR_FULL_MASK, rect_min.x, i), y_lo = __shfl_sync(GSR_FULL_MASK, rect_min.y, i);
+        const int x_hi = __shfl_sync(GSR_FULL_MASK, rect_max.x, i), y_hi = __shfl_sync(GSR_FULL_MASK, rect_max.y, i);
+        const uint32_t db = __shfl_sync(GSR_FULL_MASK, depth_bits, i);
+        const float pw = __shfl_sync(GSR_FULL_MASK, power, i);
+        const uint32_t gid = (uint32_t)(warp_first + i);
+        for (int y0 = y_lo; y0 < y_hi; y0 += 4) {
+            const int y = y0 + ty;
+            for (int x0 = x_lo; x0 < x_hi; x0 += 8) {
+                const int x = x0 + tx;
+                bool v = y < y_hi && x < x_hi && tile_hit(x, y, a.bx, a.by, c, q, pw);
+                uint64_t key = ((uint64_t)(uint32_t)(y * gridx + x) << 32) | db;
+                stage_emit(st, out, v, key, gid, lane);
+            }
+        }
+        if (lane == 0) atomicOr(&s_hit[warp], 1u << i);
+    }
+    point_valid = point_valid && !massive;
+
     const int my_tiles = point_valid ? area : 0;
     const unsigned multi = __ballot_sync(GSR_FULL_MASK, point_valid);
-    const int multi_count = __popc(multi);
-    const int max_tiles = warp_max(my_tiles);
-    if (multi_count <= 2 || max_tiles >= 32) {
-        unsigned todo = multi;
-        while (todo) {
-            const int i = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const float2 c = {__shfl_sync(GSR_FULL_MASK, point_xy.x, i), __shfl_sync(GSR_FULL_MASK, point_xy.y, i)};
-            const float3 q = {__shfl_sync(GSR_FULL_MASK, conic.x, i), __shfl_sync(GSR_FULL_MASK, conic.y, i),
-                              __shfl_sync(GSR_FULL_MASK, conic.z, i)};
-            const int x_lo = __shfl_sync(GSR_FULL_MASK, rect_min.x, i), y_lo = __shfl_sync(GSR_FULL_MASK, rect_min.y, i);
-            const int x_hi = __shfl_sync(GSR_FULL_MASK, rect_max.x, i), y_hi = __shfl_sync(GSR_FULL_MASK, rect_max.y, i);
-            const uint32_t db = __shfl_sync(GSR_FULL_MASK, depth_bits, i);
-            const float pw = __shfl_sync(GSR_FULL_MASK, power, i);
-            const uint32_t gid = (uint32_t)(warp_first + i);
-            bool any = false;
-            for (int y0 = y_lo; y0 < y_hi; y0 += 4) {
-                const int y = y0 + ty;
-                for (int x0 = x_lo; x0 < x_hi; x0 += 8) {
-                    const int x = x0 + tx;
-                    bool v = y < y_hi && x < x_hi && tile_hit(x, y, a.bx, a.by, c, q, pw);
-                    any |= v;
-                    uint64_t key = ((uint64_t)(uint32_t)(y * gridx + x) << 32) | db;
-                    stage_emit(st, out, v, key, gid, lane);
-                }
-            }
-            if (__any_sync(GSR_FULL_MASK, any) && lane == 0) atomicOr(&s_hit[warp], 1u << i);
-        }
-    } else {
+    if (multi) {
         int prefix = my_tiles;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -440,31 +492,55 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
     }
 
     // (4) block-wide final flush: one atomic per CTA.
-    if (lane == 0) s_fill[warp] = st.fill;
-    __syncthreads();
-    if (warp == 0) {
-        int f = lane < kWarps ? s_fill[lane] : 0;
-        int incl = f;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            int n = __shfl_up_sync(GSR_FULL_MASK, incl, d);
-            if ((int)lane >= d) incl += n;
+    block_flush(st, out, s_fill, s_base, lane, warp);
+}
+
+// ---------------------------------------------------------------------------
+// Queued Gaussians with large tile rectangles: persistent CTAs take one
+// Gaussian at a time and all 256 threads test its tiles, 256 per step, so a
+// screen-filling Gaussian costs ~32 steps of one CTA instead of ~255 steps of
+// one warp that also holds up its own CTA.
+__global__ __launch_bounds__(kThreads) void k_emit_massive(const PreprocessParams a)
+{
+    __shared__ uint64_t s_keys[kWarps][kStage];
+    __shared__ uint32_t s_vals[kWarps][kStage];
+    __shared__ int s_fill[kWarps];
+    __shared__ long long s_base[kWarps];
+    __shared__ int s_entry;
+    const unsigned lane = threadIdx.x & 31u;
+    const int warp = threadIdx.x >> 5;
+    Stage st{s_keys[warp], s_vals[warp], 0};
+    const EmitOut out{a.keys, a.vals, a.cap, a.counter};
+    const int count = (int)min(*a.mq.count, (uint32_t)a.mq.capacity);
+    for (;;) {
+        if (threadIdx.x == 0) s_entry = (int)atomicAdd(a.mq.head, 1u);
+        __syncthreads();
+        const int e = s_entry;
+        __syncthreads();
+        if (e >= count) break;
+        const MassiveEntry me = a.mq.entries[e];
+        const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
+        const float pw = me.ctr_power_depth.z;
+        const uint32_t db = __float_as_uint(me.ctr_power_depth.w);
+        const float3 q = {me.conic_gid.x, me.conic_gid.y, me.conic_gid.z};
+        const uint32_t gid = __float_as_uint(me.conic_gid.w);
+        const int x0 = me.rect.x, w = me.rect.y - me.rect.x, y0 = me.rect.z;
+        const int area = w * (me.rect.w - me.rect.z);
+        for (int base = 0; base < area; base += kThreads) {
+            const int t = base + (int)threadIdx.x;
+            bool v = false;
+            int x = 0, y = 0;
+            if (t < area) {
+                const int row = t / w;
+                x = x0 + (t - row * w);
+                y = y0 + row;
+                v = tile_hit(x, y, a.bx, a.by, c, q, pw);
+            }
+            uint64_t key = ((uint64_t)(uint32_t)(y * a.gx + x) << 32) | db;
+            stage_emit(st, out, v, key, gid, lane);
         }
-        int total = __shfl_sync(GSR_FULL_MASK, incl, 31);
-        long long base = 0;
-        if (lane == 0 && total > 0) base = atomicAdd(a.counter, total);
-        base = __shfl_sync(GSR_FULL_MASK, base, 0);
-        if (lane < kWarps) s_base[lane] = base + incl - f;
     }
-    __syncthreads();
-    const long long wb = s_base[warp];
-    for (int i = lane; i < st.fill; i += 32) {
-        long long pos = wb + i;
-        if (pos < a.cap) {
-            a.keys[pos] = st.k[i];
-            a.vals[pos] = st.v[i];
-        }
-    }
+    block_flush(st, out, s_fill, s_base, lane, warp);
 }
 
 // ---------------------------------------------------------------------------
@@ -558,9 +634,17 @@ cudaError_t launch_scene_prepare(int P, const float* log_scales, const float* qu
 cudaError_t launch_preprocess(const PreprocessParams& p, bool half_sh, cudaStream_t stream)
 {
     if (p.P <= 0) return cudaSuccess;
+    if (p.mq.capacity > 0) {
+        // count and head are adjacent words of the workspace header
+        cudaError_t e = cudaMemsetAsync(p.mq.count, 0, 2 * sizeof(uint32_t), stream);
+        if (e != cudaSuccess) return e;
+    }
     const int grid = div_up(p.P, kThreads);
     if (half_sh) k_preprocess<true><<<grid, kThreads, 0, stream>>>(p);
     else k_preprocess<false><<<grid, kThreads, 0, stream>>>(p);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || p.mq.capacity <= 0) return e;
+    k_emit_massive<<<device_sm_count() * 4, kThreads, 0, stream>>>(p);
     return cudaGetLastError();
 }
 

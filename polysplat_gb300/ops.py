@@ -189,11 +189,12 @@ def _preprocess(half, orig_points, shs, opacities, cov3Ds, width, height, block_
     _dev(curr_offset, "curr_offset", torch.int32)
     P = op.numel()
     cap = min(keys_u.numel(), vals_u.numel())
+    ws = _render_workspace(op.device)
     st = lib().gsr_preprocess(P, _ptr(pos), _ptr(sh), 1 if half else 0, _ptr(op), _ptr(cov), int(width), int(height),
                               int(block_x), int(block_y), _host_floats(position, 3, "position"),
                               _host_floats(rotation, 9, "rotation"), float(focal_x), float(focal_y), float(zFar),
                               float(zNear), _ptr(points_xy), _ptr(rgb_depth), _ptr(conic_opacity), _ptr(keys_u),
-                              _ptr(vals_u), cap, _ptr(curr_offset), _stream(op.device))
+                              _ptr(vals_u), cap, _ptr(curr_offset), _ptr(ws), ws.numel(), _stream(op.device))
     check(st, "preprocess")
 
 

@@ -35,7 +35,7 @@ def _declared_symbols():
     for fn in sorted(os.listdir(os.path.join(ROOT, "include"))):
         if fn.endswith(".h"):
             src = open(os.path.join(ROOT, "include", fn)).read()
-            names += re.findall(r"^\s*(?:gsr_status|size_t|int)\s+(gsr_\w+)\s*\(", src, re.M)
+            names += re.findall(r"^\s*(?:gsr_status|size_t|int|void)\s+(gsr_\w+)\s*\(", src, re.M)
     return sorted(set(names))
 
 
