@@ -524,20 +524,26 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const PreprocessParam
         const uint32_t db = __float_as_uint(me.ctr_power_depth.w);
         const float3 q = {me.conic_gid.x, me.conic_gid.y, me.conic_gid.z};
         const uint32_t gid = __float_as_uint(me.conic_gid.w);
-        const int x0 = me.rect.x, w = me.rect.y - me.rect.x, y0 = me.rect.z;
-        const int area = w * (me.rect.w - me.rect.z);
-        for (int base = 0; base < area; base += kThreads) {
-            const int t = base + (int)threadIdx.x;
-            bool v = false;
-            int x = 0, y = 0;
-            if (t < area) {
-                const int row = t / w;
-                x = x0 + (t - row * w);
-                y = y0 + row;
-                v = tile_hit(x, y, a.bx, a.by, c, q, pw);
+        // The CTA sweeps the rectangle in windows of (cols x rows) tiles, cols a
+        // power of two fitted to the rectangle's width, so narrow rectangles
+        // still fill the lanes and no per-tile integer division is needed.
+        const int x_lo = me.rect.x, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
+        const int w = x_hi - x_lo;
+        int lg = 5;
+        while (lg > 0 && (1 << (lg - 1)) >= w) lg--;
+        const int cols = 1 << lg;                // columns per warp row
+        const int rows_w = 32 >> lg;             // rows per warp
+        const int rows_cta = rows_w * kWarps;    // rows per CTA step
+        const int lx = (int)lane & (cols - 1);
+        const int ly = warp * rows_w + ((int)lane >> lg);
+        for (int wy = y_lo; wy < y_hi; wy += rows_cta) {
+            const int y = wy + ly;
+            for (int wx = x_lo; wx < x_hi; wx += cols) {
+                const int x = wx + lx;
+                const bool v = y < y_hi && x < x_hi && tile_hit(x, y, a.bx, a.by, c, q, pw);
+                uint64_t key = ((uint64_t)(uint32_t)(y * a.gx + x) << 32) | db;
+                stage_emit(st, out, v, key, gid, lane);
             }
-            uint64_t key = ((uint64_t)(uint32_t)(y * a.gx + x) << 32) | db;
-            stage_emit(st, out, v, key, gid, lane);
         }
     }
     block_flush(st, out, s_fill, s_base, lane, warp);
