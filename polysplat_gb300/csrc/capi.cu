@@ -213,13 +213,14 @@ static gsr_status preprocess_impl(int P, const float* pos, const void* shs, int 
     p.counter = curr_offset;
     p.mq.capacity = 0;
     p.mq.entries = nullptr;
-    p.mq.count = p.mq.head = nullptr;
+    p.mq.count = p.mq.head = p.mq.depth_hi = nullptr;
     if (workspace && workspace_bytes >= kSmallWorkspaceBytes) {
         WorkspaceHeader* h = reinterpret_cast<WorkspaceHeader*>(workspace);
         p.mq.entries = reinterpret_cast<MassiveEntry*>(reinterpret_cast<char*>(workspace) + kHeaderBytes);
         p.mq.capacity = kMassiveQueueEntries;
         p.mq.count = &h->mq_count;
         p.mq.head = &h->mq_head;
+        p.mq.depth_hi = &h->depth_hi;
     }
     return from_cuda(launch_preprocess(p, shs_half != 0, s));
 }
@@ -236,9 +237,9 @@ gsr_status gsr_preprocess(int P, const float* pos, const void* shs, int shs_half
                            key_capacity, curr_offset, workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
-gsr_status gsr_sort_bits(int num, const int32_t* d_num, int end_bit, void* workspace, size_t workspace_bytes,
-                         const uint64_t* keys_in, const uint32_t* values_in, uint64_t* keys_out, uint32_t* values_out,
-                         int64_t capacity, gsr_stream_t stream)
+static gsr_status sort_impl(int num, const int32_t* d_num, int end_bit, void* workspace, size_t workspace_bytes,
+                            const uint64_t* keys_in, const uint32_t* values_in, uint64_t* keys_out,
+                            uint32_t* values_out, int64_t capacity, bool compress_depth, cudaStream_t stream)
 {
     if (!workspace || end_bit < 1 || end_bit > 64 || capacity < 0 || (!d_num && num < 0)) return GSR_INVALID_ARG;
     if (!d_num && num > capacity) return GSR_INVALID_ARG;
@@ -255,7 +256,16 @@ gsr_status gsr_sort_bits(int num, const int32_t* d_num, int end_bit, void* works
     a.vals_out = values_out;
     a.ws = workspace;
     a.ws_bytes = workspace_bytes;
-    return from_cuda(launch_sort(a, (cudaStream_t)stream));
+    a.compress_depth = compress_depth;
+    return from_cuda(launch_sort(a, stream));
+}
+
+gsr_status gsr_sort_bits(int num, const int32_t* d_num, int end_bit, void* workspace, size_t workspace_bytes,
+                         const uint64_t* keys_in, const uint32_t* values_in, uint64_t* keys_out, uint32_t* values_out,
+                         int64_t capacity, gsr_stream_t stream)
+{
+    return sort_impl(num, d_num, end_bit, workspace, workspace_bytes, keys_in, values_in, keys_out, values_out,
+                     capacity, false, (cudaStream_t)stream);
 }
 
 gsr_status gsr_sort(int num, const int32_t* d_num, int width, int height, int block_x, int block_y, void* workspace,
@@ -299,7 +309,7 @@ static gsr_status render_impl(int variant, int num, const int32_t* d_num, long l
 {
     if (!workspace || !out_color || !bg_color || width <= 0 || height <= 0 || !valid_tile_shape(block_x, block_y))
         return GSR_INVALID_ARG;
-    if (render_needs_ranges(variant) ? !ranges : !keys_sorted) return GSR_INVALID_ARG;
+    if (render_needs_ranges(variant) ? !ranges : (!keys_sorted && !ranges)) return GSR_INVALID_ARG;
     if (variant < 0 || variant > GSR_RENDER_DT) return GSR_INVALID_ARG;
     RenderArgs a;
     a.variant = variant;
@@ -360,10 +370,15 @@ gsr_status gsr_forward(int variant, int P, const float* pos, const void* shs, in
     if (st != GSR_OK) return st;
     profile_mark(s);
     const int tiles = tiles_of(width, height, block_x, block_y);
-    st = gsr_sort_bits(0, curr_offset, 32 + bits_for((uint32_t)tiles), workspace, workspace_bytes, keys_unsorted,
-                       values_unsorted, keys_sorted, values_sorted, key_capacity, stream);
+    // the preprocess recorded the depth range in the workspace header: sort
+    // the (tile, depth - floor) word in as few passes as it needs
+    st = sort_impl(0, curr_offset, 32 + bits_for((uint32_t)tiles), workspace, workspace_bytes, keys_unsorted,
+                   values_unsorted, keys_sorted, values_sorted, key_capacity, true, s);
     if (st != GSR_OK) return st;
-    if (render_needs_ranges(variant)) {
+    // tile ranges by one O(M + T) pass: the caller's buffer, else the
+    // workspace's range area (too many tiles for it: the render searches)
+    if (!ranges && tiles <= kWorkspaceRangeTiles) ranges = reinterpret_cast<int32_t*>(workspace_ranges(workspace, key_capacity));
+    if (ranges) {
         e = launch_tile_ranges(0, curr_offset, key_capacity, tiles, keys_sorted, ranges, false, s);
         if (e != cudaSuccess) return from_cuda(e);
         profile_mark(s);

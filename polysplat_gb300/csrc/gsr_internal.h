@@ -16,8 +16,9 @@ struct MassiveEntry {
 struct MassiveQueue {
     MassiveEntry* entries;
     int capacity;
-    uint32_t* count;  // entries pushed (may exceed capacity: the rest were handled in place)
-    uint32_t* head;   // entries taken by the second kernel
+    uint32_t* count;     // entries pushed (may exceed capacity: the rest were handled in place)
+    uint32_t* head;      // entries taken by the second kernel
+    uint32_t* depth_hi;  // max depth bits of emitting Gaussians (for the sort's key compression)
 };
 
 struct PreprocessParams {
@@ -54,12 +55,16 @@ cudaError_t launch_scene_prepare(int P, const float* log_scales, const float* qu
 struct WorkspaceHeader {
     uint32_t status;          // OR of kErr* bits
     uint32_t render_queue;    // persistent render tile counter
-    uint32_t pass_counter[8]; // per radix pass tile counter
+    // preprocess region (cleared by every preprocess)
     uint32_t mq_count;        // massive-Gaussian queue: entries pushed
     uint32_t mq_head;         // massive-Gaussian queue: entries taken
-    uint32_t pad[4];
+    uint32_t depth_hi;        // largest depth bit pattern of an emitting Gaussian
+    uint32_t pad[3];
+    // sort region (cleared by every sort)
+    uint32_t pass_counter[8]; // per radix pass tile counter
     uint32_t hist[8][256];    // per-pass digit histograms
 };
+constexpr size_t kSortRegionOffset = 8 * sizeof(uint32_t);
 constexpr size_t kHeaderBytes = 16384;
 static_assert(sizeof(WorkspaceHeader) <= kHeaderBytes, "header too large");
 
@@ -72,17 +77,31 @@ constexpr size_t kMassiveQueueBytes = (size_t)kMassiveQueueEntries * sizeof(Mass
 constexpr size_t kSmallWorkspaceBytes = kHeaderBytes + kMassiveQueueBytes;
 
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
-constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per tile
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 2048 keys per tile
 constexpr int kMaxPasses = 8;
 
 size_t sort_workspace_bytes(long long cap);
+// Tile-range area at the end of a full workspace (frames of up to
+// kWorkspaceRangeTiles tiles; the fused forward uses it when the caller
+// passes no ranges buffer).
+constexpr int kWorkspaceRangeTiles = 1 << 20;
+int2* workspace_ranges(void* ws, long long cap);
+
+// Lower bound of the depth bit patterns of emitted keys: view depth is > 0.2
+// (preprocess.cu:363), so every key's low word exceeds the bits of 0.2f.
+constexpr uint32_t kDepthBitsFloor = 0x3E4CCCCDu;
 
 struct SortArgs {
     int num;                // host count (used when d_num == nullptr)
     const int32_t* d_num;   // device count or nullptr
     long long cap;          // capacity of the key buffers
     int end_bit;
+    // Depth compression (fused forward only): order by
+    // (tile << nb) | (low word - kDepthBitsFloor) with nb = bits(depth_hi -
+    // floor), taken from the workspace header the preprocess filled.  Same
+    // order as the full key for every key the preprocess emits.
+    bool compress_depth;
     const uint64_t* keys_in;
     const uint32_t* vals_in;
     uint64_t* keys_out;

@@ -307,6 +307,7 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
     __shared__ int s_fill[kWarps];
     __shared__ long long s_base[kWarps];
     __shared__ uint32_t s_hit[kWarps];
+    __shared__ int s_pref[kWarps][32];
 
     const unsigned lane = threadIdx.x & 31u;
     const int warp = threadIdx.x >> 5;
@@ -440,20 +441,21 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
             if ((int)lane >= d) prefix += n;
         }
         const int total = __shfl_sync(GSR_FULL_MASK, prefix, 31);
+        s_pref[warp][lane] = prefix;  // inclusive prefix of the tile counts
+        __syncwarp();
         prefix -= my_tiles;
-        const int default_owner = __ffs(multi) - 1;
         for (int base = 0; base < total; base += 32) {
             const int task = base + (int)lane;
             const bool task_ok = task < total;
-            int owner = default_owner;
-            unsigned bits = multi;
-            while (bits) {
-                const int cand = __ffs(bits) - 1;
-                const int cp = __shfl_sync(GSR_FULL_MASK, prefix, cand);
-                const int cc = __shfl_sync(GSR_FULL_MASK, my_tiles, cand);
-                if (task_ok && task >= cp && task < cp + cc) owner = cand;
-                bits &= bits - 1;
+            // owner = first lane whose inclusive prefix exceeds the task index
+            int lo = 0, hi = 31;
+#pragma unroll
+            for (int step = 0; step < 5; step++) {
+                const int mid = (lo + hi) >> 1;
+                if (s_pref[warp][mid] > task) hi = mid;
+                else lo = mid + 1;
             }
+            const int owner = task_ok ? lo : __ffs(multi) - 1;
             const int ox = __shfl_sync(GSR_FULL_MASK, rect_min.x, owner);
             const int oy = __shfl_sync(GSR_FULL_MASK, rect_min.y, owner);
             const int ow = __shfl_sync(GSR_FULL_MASK, rect_max.x, owner) - ox;
@@ -482,6 +484,10 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
 
     // (3) render features for every Gaussian that emitted at least one key.
     const bool emitted = (s_hit[warp] >> lane) & 1u;
+    if (a.mq.depth_hi) {
+        const uint32_t m = __reduce_max_sync(GSR_FULL_MASK, emitted ? depth_bits : 0u);
+        if (lane == 0 && m) atomicMax(a.mq.depth_hi, m);
+    }
     if (emitted) {
         a.points_xy[idx] = point_xy;
         a.conic_opacity[idx] = make_float4((-0.5f * kLog2e) * conic.x, -kLog2e * conic.y, (-0.5f * kLog2e) * conic.z,
@@ -500,6 +506,51 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
 // Gaussian at a time and all 256 threads test its tiles, 256 per step, so a
 // screen-filling Gaussian costs ~32 steps of one CTA instead of ~255 steps of
 // one warp that also holds up its own CTA.
+constexpr int kMaxBandRows = 1024;  // tile rows of a rectangle that get candidate bands
+
+// Per-Gaussian constants of the ellipse A dx^2 + 2B dx dy + C dy^2 <= w,
+// derived in double from the FP32 conic (det = AC - B^2 is where cancellation
+// would hurt), then used in float per tile row.
+struct Band {
+    float A, B, Aw, det, dymax, dxmax, dyr, cx, cy, m;
+};
+
+__device__ __forceinline__ Band make_band(double A, double B, double C, double w, double det, float cx, float cy,
+                                          float m)
+{
+    Band b;
+    b.A = (float)A;
+    b.B = (float)B;
+    b.Aw = (float)(A * w);
+    b.det = (float)det;
+    b.dymax = (float)sqrt(w * A / det);
+    b.dxmax = (float)sqrt(w * C / det);
+    b.dyr = (float)(-B * sqrt(w / (C * det)));  // dy where the ellipse reaches its largest x
+    b.cx = cx;
+    b.cy = cy;
+    b.m = m;
+    return b;
+}
+
+// Candidate tile columns of tile row `ty`: the ellipse's x-extent over the
+// row's pixel band, widened by m pixels on every side.  False when the
+// widened band misses the ellipse.
+__device__ __forceinline__ bool band_columns(const Band& e, int ty, int by, int bx, int x_lo, int x_hi, int& c_lo,
+                                             int& c_hi)
+{
+    const float p = fmaxf((float)(ty * by) - e.m - e.cy, -e.dymax);
+    const float q = fminf((float)(ty * by + by - 1) + e.m - e.cy, e.dymax);
+    if (p > q) return false;
+    auto half = [&](float dy) { return sqrtf(fmaxf(0.0f, e.Aw - e.det * dy * dy)); };
+    const float hp = half(p), hq = half(q);
+    const float xr = (e.dyr >= p && e.dyr <= q) ? e.dxmax : fmaxf((-e.B * p + hp) / e.A, (-e.B * q + hq) / e.A);
+    const float xl = (-e.dyr >= p && -e.dyr <= q) ? -e.dxmax : fminf((-e.B * p - hp) / e.A, (-e.B * q - hq) / e.A);
+    const float lo = floorf((e.cx + xl - e.m) / (float)bx), hi = floorf((e.cx + xr + e.m) / (float)bx);
+    c_lo = (int)fmaxf((float)x_lo, lo);
+    c_hi = (int)fminf((float)(x_hi - 1), hi);
+    return c_lo <= c_hi;
+}
+
 __global__ __launch_bounds__(kThreads) void k_emit_massive(const PreprocessParams a)
 {
     __shared__ uint64_t s_keys[kWarps][kStage];
@@ -507,6 +558,7 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const PreprocessParam
     __shared__ int s_fill[kWarps];
     __shared__ long long s_base[kWarps];
     __shared__ int s_entry;
+    __shared__ short2 s_band[kMaxBandRows];
     const unsigned lane = threadIdx.x & 31u;
     const int warp = threadIdx.x >> 5;
     Stage st{s_keys[warp], s_vals[warp], 0};
@@ -524,11 +576,49 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const PreprocessParam
         const uint32_t db = __float_as_uint(me.ctr_power_depth.w);
         const float3 q = {me.conic_gid.x, me.conic_gid.y, me.conic_gid.z};
         const uint32_t gid = __float_as_uint(me.conic_gid.w);
-        // The CTA sweeps the rectangle in windows of (cols x rows) tiles, cols a
-        // power of two fitted to the rectangle's width, so narrow rectangles
-        // still fill the lanes and no per-tile integer division is needed.
         const int x_lo = me.rect.x, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
         const int w = x_hi - x_lo;
+
+        // Well-conditioned ellipses: only tiles within two tiles of the
+        // ellipse's exact extent in each tile row get the (exact, FP32) test;
+        // tiles farther out cannot pass it.  The float evaluation error of the
+        // test stays far below that margin while det/(AC) > 1e-6 (worst case a
+        // few pixels at 8K); below that, or for non-finite values, every tile
+        // of the rectangle is tested.
+        const double A = q.x, B = q.y, C = q.z, W2 = 2.0 * (double)pw;
+        const double det = A * C - B * B;
+        const bool banded = (y_hi - y_lo) <= kMaxBandRows && A > 0.0 && C > 0.0 && W2 > 0.0 &&
+                            det > 1e-6 * A * C && isfinite(det) && isfinite(W2) && isfinite((double)c.x) &&
+                            isfinite((double)c.y);
+        if (banded) {
+            const Band eb = make_band(A, B, C, W2, det, c.x, c.y, 2.0f * (float)max(a.bx, a.by));
+            for (int r = threadIdx.x; r < y_hi - y_lo; r += kThreads) {
+                int clo = 0, chi = -1;
+                if (!band_columns(eb, y_lo + r, a.by, a.bx, x_lo, x_hi, clo, chi)) {
+                    clo = 0;
+                    chi = -1;
+                }
+                s_band[r] = make_short2((short)clo, (short)chi);
+            }
+            __syncthreads();
+            for (int r = warp; r < y_hi - y_lo; r += kWarps) {
+                const short2 band = s_band[r];
+                const int y = y_lo + r;
+                for (int x0 = band.x; x0 <= band.y; x0 += 32) {
+                    const int x = x0 + (int)lane;
+                    const bool v = x <= band.y && tile_hit(x, y, a.bx, a.by, c, q, pw);
+                    uint64_t key = ((uint64_t)(uint32_t)(y * a.gx + x) << 32) | db;
+                    stage_emit(st, out, v, key, gid, lane);
+                }
+            }
+            __syncthreads();  // s_band is rewritten by the next entry
+            continue;
+        }
+
+        // Otherwise the CTA sweeps the rectangle in windows of (cols x rows)
+        // tiles, cols a power of two fitted to the rectangle's width, so narrow
+        // rectangles still fill the lanes and no per-tile integer division is
+        // needed.
         int lg = 5;
         while (lg > 0 && (1 << (lg - 1)) >= w) lg--;
         const int cols = 1 << lg;                // columns per warp row
@@ -641,8 +731,8 @@ cudaError_t launch_preprocess(const PreprocessParams& p, bool half_sh, cudaStrea
 {
     if (p.P <= 0) return cudaSuccess;
     if (p.mq.capacity > 0) {
-        // count and head are adjacent words of the workspace header
-        cudaError_t e = cudaMemsetAsync(p.mq.count, 0, 2 * sizeof(uint32_t), stream);
+        // count, head and depth_hi are adjacent words of the workspace header
+        cudaError_t e = cudaMemsetAsync(p.mq.count, 0, 3 * sizeof(uint32_t), stream);
         if (e != cudaSuccess) return e;
     }
     const int grid = div_up(p.P, kThreads);

@@ -349,14 +349,23 @@ template <int BX, int BY>
 cudaError_t dispatch_shape(int variant, bool tma, const RenderParams& p, cudaStream_t stream)
 {
     constexpr int SH = (BX == 16 && BY == 16) ? 0 : 1;
+    // FUSED/DEFAULT find their ranges in-kernel unless ranges were supplied
+    // (the same [lower, upper) bounds, so the same image)
+    const bool ranges = p.ranges != nullptr;
     switch (variant) {
     case GSR_RENDER_PERSISTENT_RANGES:
         return tma ? launch_variant<BX, BY, 8, 0, false, 0, true>(p, stream)
                    : launch_variant<BX, BY, 8, 0, false, 0, false>(p, stream);
     case GSR_RENDER_PERSISTENT_FUSED:
+        if (ranges)
+            return tma ? launch_variant<BX, BY, 16, 0, false, 0, true>(p, stream)
+                       : launch_variant<BX, BY, 16, 0, false, 0, false>(p, stream);
         return tma ? launch_variant<BX, BY, 16, 0, false, 1, true>(p, stream)
                    : launch_variant<BX, BY, 16, 0, false, 1, false>(p, stream);
     case GSR_RENDER_DEFAULT:
+        if (ranges)
+            return tma ? launch_variant<BX, BY, 2, SH, false, 0, true>(p, stream)
+                       : launch_variant<BX, BY, 2, SH, false, 0, false>(p, stream);
         return tma ? launch_variant<BX, BY, 2, SH, false, 1, true>(p, stream)
                    : launch_variant<BX, BY, 2, SH, false, 1, false>(p, stream);
     case GSR_RENDER_RANGES_CADENCE2:

@@ -9,12 +9,23 @@
 // Structure (one-sweep radix sort with decoupled look-back):
 //   1. k_upsweep: one read of all keys builds the 256-bin histogram of every
 //      8-bit digit pass at once, and clears the first look-back array.
-//   2. k_pass (one launch per digit): persistent CTAs take 4096-key tiles in
+//   2. k_pass (one launch per digit): persistent CTAs take 2048-key tiles in
 //      order from an atomic counter, rank keys stably inside the tile (per-warp
-//      ballot ranking), publish per-digit tile counts, look back over earlier
-//      tiles for the running per-digit prefix (bounded spin), reorder the tile
-//      in shared memory by digit and write it out with coalesced stores.
+//      ranking by match.any or by bit ballots), publish per-digit tile counts,
+//      look back over earlier tiles for the running per-digit prefix (bounded
+//      spin, four predecessors per round trip), reorder the tile in shared
+//      memory by digit and write it out with coalesced stores.
+//
+// Depth compression (fused forward): every emitted key has a low word above
+// the bits of 0.2f and at most the header's depth_hi, so ordering by
+// (tile << nb) | (low - floor) with nb = bits(depth_hi - floor) is the same
+// order in fewer bits.  The number of passes that do work is then decided on
+// the device; the remaining launches return at once, and each pass picks its
+// source and destination buffer so that the last working pass lands in the
+// output.
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 
 #include "gsr_internal.h"
 
@@ -25,7 +36,7 @@ constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
 constexpr int kWarpsPerCta = kSortThreads / 32;
-constexpr int kWarpItems = kSortItems * 32;  // 512 consecutive keys per warp
+constexpr int kWarpItems = kSortItems * 32;  // consecutive keys per warp
 
 __device__ __forceinline__ int sort_count(const SortArgs& a)
 {
@@ -62,18 +73,55 @@ __host__ __device__ inline Layout make_layout(void* ws, long long cap)
     return L;
 }
 
+// The ordering word of a key and the number of its bits that matter.
+struct KeyMap {
+    int bits;           // significant bits of the ordering word
+    int depth_bits;     // 0: no compression
+    uint64_t mask;      // mask of the uncompressed key (end_bit bits)
+    uint32_t tile_mask;
+};
+
+__device__ __forceinline__ KeyMap key_map(const SortArgs& a, const Layout& L)
+{
+    KeyMap m;
+    m.mask = a.end_bit >= 64 ? ~0ull : ((1ull << a.end_bit) - 1ull);
+    m.depth_bits = 0;
+    m.tile_mask = 0;
+    m.bits = a.end_bit;
+    if (a.compress_depth && a.end_bit > 32) {
+        const uint32_t hi = L.hdr->depth_hi;
+        const int nb = hi > kDepthBitsFloor ? bits_for(hi - kDepthBitsFloor) : 0;
+        m.depth_bits = nb;
+        m.tile_mask = (uint32_t)((1ull << (a.end_bit - 32)) - 1ull);
+        m.bits = (a.end_bit - 32) + nb;
+        if (m.bits < 1) m.bits = 1;
+    }
+    return m;
+}
+
+__device__ __forceinline__ uint64_t order_word(uint64_t k, const KeyMap& m)
+{
+    if (m.tile_mask == 0) return k & m.mask;
+    const uint64_t tile = (uint64_t)((uint32_t)(k >> 32) & m.tile_mask);
+    return (tile << m.depth_bits) | (uint64_t)((uint32_t)k - kDepthBitsFloor);
+}
+
+__device__ __forceinline__ int passes_of(const KeyMap& m) { return (m.bits + 7) / 8; }
+
 // ---------------------------------------------------------------------------
 // Histogram of every digit pass.  Each thread takes runs of 8 consecutive keys
 // and merges equal consecutive digits before touching shared memory: keys of
 // one Gaussian are emitted together and share their depth digits, so this
 // removes most same-address shared atomics.
-__global__ __launch_bounds__(256) void k_upsweep(SortArgs a, Layout L, int passes)
+__global__ __launch_bounds__(256) void k_upsweep(SortArgs a, Layout L, int max_passes)
 {
     __shared__ uint32_t s_hist[kMaxPasses][256];
     for (int i = threadIdx.x; i < kMaxPasses * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0u;
     __syncthreads();
     const int n = sort_count(a);
     const int tiles = (n + kSortTile - 1) / kSortTile;
+    const KeyMap km = key_map(a, L);
+    const int passes = min(max_passes, passes_of(km));
     // clear the look-back state used by the first digit pass
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)tiles * 256;
          i += (long long)gridDim.x * blockDim.x)
@@ -97,16 +145,16 @@ __global__ __launch_bounds__(256) void k_upsweep(SortArgs a, Layout L, int passe
 #pragma unroll
             for (int j = 0; j < 8; j++) k[j] = j < cnt ? __ldg(a.keys_in + b + j) : 0ull;
         }
+#pragma unroll
+        for (int j = 0; j < 8; j++) k[j] = order_word(k[j], km);
         for (int p = 0; p < passes; p++) {
             const int shift = 8 * p;
-            const int bits = min(8, a.end_bit - shift);
-            const uint32_t mask = (1u << bits) - 1u;
-            uint32_t cur = (uint32_t)(k[0] >> shift) & mask;
+            uint32_t cur = (uint32_t)(k[0] >> shift) & 0xFFu;
             uint32_t run = 1;
 #pragma unroll
             for (int j = 1; j < 8; j++) {
                 if (j >= cnt) break;
-                uint32_t d = (uint32_t)(k[j] >> shift) & mask;
+                uint32_t d = (uint32_t)(k[j] >> shift) & 0xFFu;
                 if (d == cur) {
                     run++;
                 } else {
@@ -138,7 +186,7 @@ struct PassSmem {
 };
 
 // Exclusive scan of 256 values held one per thread (blockDim == 256).
-__device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* warp_sums, uint32_t& total)
+__device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* warp_sums)
 {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     uint32_t incl = v;
@@ -149,44 +197,58 @@ __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* war
     }
     if (lane == 31) warp_sums[warp] = incl;
     __syncthreads();
-    uint32_t wpre = 0, tot = 0;
+    uint32_t wpre = 0;
 #pragma unroll
-    for (int w = 0; w < kWarpsPerCta; w++) {
-        uint32_t s = warp_sums[w];
-        if (w < (int)warp) wpre += s;
-        tot += s;
-    }
-    total = tot;
+    for (int w = 0; w < kWarpsPerCta; w++)
+        if (w < (int)warp) wpre += warp_sums[w];
     __syncthreads();
     return wpre + incl - v;
 }
 
-__global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortArgs a, Layout L, int pass, int passes,
-                                                          const uint64_t* __restrict__ kin,
-                                                          const uint32_t* __restrict__ vin, uint64_t* kout,
-                                                          uint32_t* vout)
+struct PassBuffers {
+    const uint64_t* keys_in;
+    const uint32_t* vals_in;
+    uint64_t* keys_out;
+    uint32_t* vals_out;
+    uint64_t* keys_alt;
+    uint32_t* vals_alt;
+};
+
+// MATCH: per-warp ranking with match.any (one instruction per key);
+// otherwise with one ballot per digit bit.
+template <bool MATCH>
+__global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortArgs a, Layout L, int pass, PassBuffers B)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PassSmem& S = *reinterpret_cast<PassSmem*>(smem_raw);
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const KeyMap km = key_map(a, L);
+    const int passes = passes_of(km);
+    if (pass >= passes) return;  // nothing left to order in this digit
     const int n = sort_count(a);
     const int tiles = (n + kSortTile - 1) / kSortTile;
     const int shift = 8 * pass;
-    const int bits = min(8, a.end_bit - shift);
-    const uint32_t dmask = (1u << bits) - 1u;
+    const int bits = min(8, km.bits - shift);
+    // ping-pong so that the last working pass writes the output buffers
+    const bool to_out = ((passes - 1 - pass) & 1) == 0;
+    const uint64_t* kin = B.keys_in;
+    const uint32_t* vin = B.vals_in;
+    if (pass > 0) {
+        const bool prev_out = ((passes - pass) & 1) == 0;
+        kin = prev_out ? B.keys_out : B.keys_alt;
+        vin = prev_out ? B.vals_out : B.vals_alt;
+    }
+    uint64_t* kout = to_out ? B.keys_out : B.keys_alt;
+    uint32_t* vout = to_out ? B.vals_out : B.vals_alt;
     uint32_t* look = L.look[pass & 1];
     uint32_t* look_next = L.look[(pass + 1) & 1];
     const bool clear_next = pass + 1 < passes;
 
-    // global digit starts for this pass
-    {
-        uint32_t tot;
-        uint32_t h = L.hdr->hist[pass][threadIdx.x];
-        S.gstart[threadIdx.x] = block_excl_scan256(h, S.warp_sums, tot);
-    }
+    S.gstart[threadIdx.x] = block_excl_scan256(L.hdr->hist[pass][threadIdx.x], S.warp_sums);
 
     for (;;) {
         if (threadIdx.x == 0) S.tile = (int)atomicAdd(&L.hdr->pass_counter[pass], 1u);
+        for (int i = threadIdx.x; i < kWarpsPerCta * 256; i += kSortThreads) (&S.whist[0][0])[i] = 0u;
         __syncthreads();
         const int tile = S.tile;
         if (tile >= tiles) break;
@@ -194,12 +256,10 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortArgs a, Layout L, 
         const int tcount = (int)min((long long)kSortTile, (long long)n - tbase);
         if (clear_next) look_next[(size_t)tile * 256 + threadIdx.x] = 0u;
 
-        // ---- load + rank (warp-contiguous chunk of 512 keys) ----
-        for (int i = threadIdx.x; i < kWarpsPerCta * 256; i += kSortThreads) (&S.whist[0][0])[i] = 0u;
-        __syncwarp();
-        __syncthreads();
+        // ---- load (warp-contiguous chunk) + stable per-warp rank ----
         uint64_t key[kSortItems];
         uint32_t val[kSortItems];
+        uint32_t dig[kSortItems];
         uint32_t rank[kSortItems];
         const int wbase = (int)warp * kWarpItems;
 #pragma unroll
@@ -217,19 +277,33 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortArgs a, Layout L, 
         for (int i = 0; i < kSortItems; i++) {
             const int o = wbase + i * 32 + (int)lane;
             const bool ok = o < tcount;
-            const uint32_t d = (uint32_t)(key[i] >> shift) & dmask;
-            unsigned peers = __ballot_sync(GSR_FULL_MASK, ok);
-            for (int b = 0; b < bits; b++) {
-                const bool bit = (d >> b) & 1u;
-                const unsigned bb = __ballot_sync(GSR_FULL_MASK, bit);
-                peers &= bit ? bb : ~bb;
+            const uint32_t d = (uint32_t)(order_word(key[i], km) >> shift) & ((1u << bits) - 1u);
+            dig[i] = d;
+            if (MATCH) {
+                // out-of-range lanes get a value no real digit has
+                const unsigned peers = __match_any_sync(GSR_FULL_MASK, ok ? d : 0x100u + lane);
+                const int leader = __ffs(peers) - 1;
+                uint32_t base = 0;
+                if (ok && (int)lane == leader) {
+                    base = S.whist[warp][d];
+                    S.whist[warp][d] = base + __popc(peers);
+                }
+                base = __shfl_sync(GSR_FULL_MASK, base, leader);
+                rank[i] = base + __popc(peers & lanemask_lt());
+            } else {
+                unsigned peers = __ballot_sync(GSR_FULL_MASK, ok);
+                for (int b = 0; b < bits; b++) {
+                    const bool bit = (d >> b) & 1u;
+                    const unsigned bb = __ballot_sync(GSR_FULL_MASK, bit);
+                    peers &= bit ? bb : ~bb;
+                }
+                uint32_t base = 0;
+                if (ok) base = S.whist[warp][d];
+                __syncwarp();
+                if (ok && (lane == (unsigned)(__ffs(peers) - 1))) S.whist[warp][d] = base + __popc(peers);
+                __syncwarp();
+                rank[i] = base + __popc(peers & lanemask_lt());
             }
-            uint32_t base = 0;
-            if (ok) base = S.whist[warp][d];
-            __syncwarp();
-            if (ok && (lane == (unsigned)(__ffs(peers) - 1))) S.whist[warp][d] = base + __popc(peers);
-            __syncwarp();
-            rank[i] = base + __popc(peers & lanemask_lt());
         }
         __syncthreads();
 
@@ -245,8 +319,7 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortArgs a, Layout L, 
                 run += c;
             }
             dtot = run;
-            uint32_t total;
-            S.digit_excl[d] = block_excl_scan256(run, S.warp_sums, total);
+            S.digit_excl[d] = block_excl_scan256(run, S.warp_sums);
         }
 
         // ---- decoupled look-back: thread d owns digit d ----
@@ -263,7 +336,8 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortArgs a, Layout L, 
             while (!done) {
                 uint32_t v[4];
 #pragma unroll
-                for (int k = 0; k < 4; k++) v[k] = (j - k >= 0) ? ld_relaxed_u32(look + (size_t)(j - k) * 256 + d) : kFlagPrefix;
+                for (int k = 0; k < 4; k++)
+                    v[k] = (j - k >= 0) ? ld_relaxed_u32(look + (size_t)(j - k) * 256 + d) : kFlagPrefix;
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     if (done) break;
@@ -290,8 +364,7 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortArgs a, Layout L, 
         for (int i = 0; i < kSortItems; i++) {
             const int o = wbase + i * 32 + (int)lane;
             if (o < tcount) {
-                const uint32_t d = (uint32_t)(key[i] >> shift) & dmask;
-                const uint32_t pos = S.digit_excl[d] + S.whist[warp][d] + rank[i];
+                const uint32_t pos = S.digit_excl[dig[i]] + S.whist[warp][dig[i]] + rank[i];
                 S.keys[pos] = key[i];
                 S.vals[pos] = val[i];
             }
@@ -300,7 +373,7 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortArgs a, Layout L, 
         bool oob = false;
         for (int p = threadIdx.x; p < tcount; p += kSortThreads) {
             const uint64_t k = S.keys[p];
-            const uint32_t d = (uint32_t)(k >> shift) & dmask;
+            const uint32_t d = (uint32_t)(order_word(k, km) >> shift) & ((1u << bits) - 1u);
             const long long g = (long long)S.gofs[d] + p;
             if (g < 0 || g >= n) {  // only after a look-back timeout: never write outside the buffer
                 oob = true;
@@ -314,25 +387,43 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortArgs a, Layout L, 
     }
 }
 
+bool use_match_ranking()
+{
+    static int mode = -1;
+    if (mode < 0) {
+        const char* e = getenv("GSR_SORT_RANK");
+        mode = (e && strcmp(e, "ballot") == 0) ? 0 : 1;
+    }
+    return mode == 1;
+}
+
 }  // namespace
 
-size_t sort_workspace_bytes(long long cap)
+static size_t sort_area_bytes(long long cap)
 {
     if (cap < 1) cap = 1;
     long long tiles = (cap + kSortTile - 1) / kSortTile;
-    return kSmallWorkspaceBytes + align256((size_t)cap * 8) + align256((size_t)cap * 4) + 2 * align256((size_t)tiles * 256 * 4);
+    return kSmallWorkspaceBytes + align256((size_t)cap * 8) + align256((size_t)cap * 4) +
+           2 * align256((size_t)tiles * 256 * 4);
+}
+
+size_t sort_workspace_bytes(long long cap) { return sort_area_bytes(cap) + (size_t)kWorkspaceRangeTiles * 8; }
+
+int2* workspace_ranges(void* ws, long long cap)
+{
+    return reinterpret_cast<int2*>(reinterpret_cast<char*>(ws) + sort_area_bytes(cap));
 }
 
 cudaError_t launch_sort(const SortArgs& a, cudaStream_t stream)
 {
     if (a.end_bit < 1 || a.end_bit > 64) return cudaErrorInvalidValue;
-    if (a.ws_bytes < sort_workspace_bytes(a.cap)) return cudaErrorInvalidValue;
+    if (a.ws_bytes < sort_area_bytes(a.cap)) return cudaErrorInvalidValue;
     if (a.cap >= (1LL << 30)) return cudaErrorInvalidValue;
     Layout L = make_layout(a.ws, a.cap);
-    const int passes = (a.end_bit + 7) / 8;
-    // clear counters and histograms, keep the status word
-    cudaError_t e = cudaMemsetAsync(reinterpret_cast<char*>(L.hdr) + sizeof(uint32_t), 0,
-                                    sizeof(WorkspaceHeader) - sizeof(uint32_t), stream);
+    const int passes = (a.end_bit + 7) / 8;  // upper bound; the device may need fewer
+    // clear the sort region of the header (pass counters and histograms)
+    cudaError_t e = cudaMemsetAsync(reinterpret_cast<char*>(L.hdr) + kSortRegionOffset, 0,
+                                    sizeof(WorkspaceHeader) - kSortRegionOffset, stream);
     if (e != cudaSuccess) return e;
     const int sms = device_sm_count();
     const long long tiles_cap = L.tiles_cap;
@@ -341,28 +432,24 @@ cudaError_t launch_sort(const SortArgs& a, cudaStream_t stream)
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     profile_mark(stream);
 
-    static bool attr_set = false;
+    const bool match = use_match_ranking();
+    auto kern = match ? k_pass<true> : k_pass<false>;
+    static bool attr_set[2] = {false, false};
     const int smem = (int)sizeof(PassSmem);
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        attr_set = true;
+    if (!attr_set[match]) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr_set[match] = true;
     }
-    const int grid = (int)std::min<long long>((long long)sms * 2, std::max<long long>(1, tiles_cap));
+    static int per_sm[2] = {0, 0};
+    if (per_sm[match] == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kSortThreads, smem) != cudaSuccess || b < 1) b = 1;
+        per_sm[match] = b;
+    }
+    const int grid = (int)std::min<long long>((long long)sms * per_sm[match], std::max<long long>(1, tiles_cap));
+    PassBuffers B{a.keys_in, a.vals_in, a.keys_out, a.vals_out, L.alt_keys, L.alt_vals};
     for (int p = 0; p < passes; p++) {
-        const bool to_out = ((passes - 1 - p) % 2) == 0;
-        const uint64_t* kin;
-        const uint32_t* vin;
-        if (p == 0) {
-            kin = a.keys_in;
-            vin = a.vals_in;
-        } else {
-            const bool prev_out = ((passes - p) % 2) == 0;
-            kin = prev_out ? a.keys_out : L.alt_keys;
-            vin = prev_out ? a.vals_out : L.alt_vals;
-        }
-        uint64_t* ko = to_out ? a.keys_out : L.alt_keys;
-        uint32_t* vo = to_out ? a.vals_out : L.alt_vals;
-        k_pass<<<grid, kSortThreads, smem, stream>>>(a, L, p, passes, kin, vin, ko, vo);
+        kern<<<grid, kSortThreads, smem, stream>>>(a, L, p, B);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         profile_mark(stream);
     }

@@ -196,6 +196,8 @@ def workload(name: str):
         return scene_clustered(), [camera_front(1920, 1080, 1400.0)]
     if name == "city_20m_8k":
         return scene_city(), [camera_city()]
+    if name == "clustered_1m_1080p":  # a third-size plain_3m_1080p, for profiling captures
+        return scene_clustered(1_000_000, seed=1), [camera_front(1920, 1080, 1400.0)]
     if name == "diff_1m_8cam":
         scene = scene_plain_small(1_000_000, seed=4, mean_sigma=3.0)
         cams = [orbit_camera(10.0, 2 * math.pi * k / 8, 0.0, 1280, 720, 900.0, id=k) for k in range(8)]
