@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--quick", action="store_true",
                     help="device-timed frames only (no e2e, CPU baseline or reference pipeline): for profiling")
     ap.add_argument("--cap-log2", type=int, default=0, help="key-buffer capacity 2^n (default: by scene size)")
+    ap.add_argument("--pipeline", default="single", choices=["single", "depth_first"],
+                    help="single-pass 64-bit key sort, or depth sort + 32-bit tile sort")
     return ap.parse_args()
 
 
@@ -223,7 +225,23 @@ def run_gsr(args):
     ws = rast.list_sorting_space
     wsb = ws.numel()
 
-    def frame():
+    df = args.pipeline == "depth_first"
+    scratch = None
+    if df:
+        scratch = torch.zeros(ops.depth_first_scratch_size(scene.num_vertex), dtype=torch.int8, device=dev)
+
+    def frame_df():
+        st = L.gsr_forward_depth_first(
+            1, scene.num_vertex, scene.position.data_ptr(), scene.shs_half.data_ptr(), 1, scene.opacity.data_ptr(),
+            scene.cov3d.data_ptr(), cam.width, cam.height, 16, 16, cam_pos, cam_rot, cam.focal_x, cam.focal_y,
+            cam.zFar, cam.zNear, rast.curr_offset.data_ptr(), ws.data_ptr(), wsb, scratch.data_ptr(),
+            scratch.numel(), rast.gaussian_keys_unsorted.data_ptr(), rast.gaussian_values_unsorted.data_ptr(),
+            rast.gaussian_keys_sorted.data_ptr(), rast.gaussian_values_sorted.data_ptr(), cap,
+            rast.points_xy.data_ptr(), rast.rgb_depth.data_ptr(), rast.conic_opacity.data_ptr(), None, bgc,
+            out.data_ptr(), sh)
+        check(st, "forward_depth_first")
+
+    def frame_single():
         st = L.gsr_forward(1, scene.num_vertex, scene.position.data_ptr(), scene.shs_half.data_ptr(), 1,
                            scene.opacity.data_ptr(), scene.cov3d.data_ptr(), cam.width, cam.height, 16, 16, cam_pos,
                            cam_rot, cam.focal_x, cam.focal_y, cam.zFar, cam.zNear, rast.curr_offset.data_ptr(),
@@ -233,12 +251,14 @@ def run_gsr(args):
                            rast.rgb_depth.data_ptr(), rast.conic_opacity.data_ptr(), None, bgc, out.data_ptr(), sh)
         check(st, "forward")
 
+    frame = frame_df if df else frame_single
     for _ in range(max(3, args.warmup)):
         frame()
     num = ops._read_status(ws, rast.curr_offset, cap, "forward")
     tiles = ((cam.width + 15) // 16) * ((cam.height + 15) // 16)
     end_bit = 32 + tiles.bit_length()
     passes = (end_bit + 7) // 8
+    tile_passes = (tiles.bit_length() + 7) // 8
 
     # stage events recorded by the library: [preprocess, upsweep, pass 0..passes-1, render]
     K = args.steps
@@ -271,21 +291,31 @@ def run_gsr(args):
         elapsed_ms = float(t.item())
     fps = world * K / (elapsed_ms / 1000.0)
 
-    stage_names = (["preprocess", "sort_upsweep"] + ["sort_pass%d" % p for p in range(passes)]
-                   + ["tile_ranges", "render"])
+    if df:
+        stage_names = (["preprocess", "compact", "depth_upsweep"] + ["depth_pass%d" % p for p in range(4)]
+                       + ["offsets", "emit", "tile_upsweep"] + ["tile_pass%d" % p for p in range(tile_passes)]
+                       + ["tile_ranges", "render"])
+    else:
+        stage_names = (["preprocess", "sort_upsweep"] + ["sort_pass%d" % p for p in range(passes)]
+                       + ["tile_ranges", "render"])
     if n_stages != len(stage_names):
         raise RuntimeError("expected %d timed stages, the library recorded %d" % (len(stage_names), n_stages))
     stage_avg = {nm: statistics.mean(ms_buf[f * MAXS + i] for f in range(K)) for i, nm in enumerate(stage_names)}
     # passes the depth compression made unnecessary return at once
-    pass_ms = [stage_avg["sort_pass%d" % p] for p in range(passes)]
+    pass_key = "tile_pass" if df else "sort_pass"
+    pass_ms = [stage_avg["%s%d" % (pass_key, p)] for p in range(tile_passes if df else passes)]
     working = [t for t in pass_ms if t > 0.2 * max(pass_ms)]
     pass_avg = statistics.mean(working)
 
     # algorithmic bytes per launch (formulas in the design doc)
     P = scene.num_vertex
     peak, peak_kind = measured_peaks()
-    pass_bytes = 24.0 * num  # read key+value, write key+value
-    pre_bytes = P * (12 + 4 + 24 + 96) + num * 12
+    # a digit pass reads and writes every (key, value) pair: 12-byte pairs in
+    # the single-pass sort, 8-byte (tile id, value) pairs in the depth-first one
+    pass_bytes = (16.0 if df else 24.0) * num
+    # preprocess: scene read + features of emitters + keys (the counting pass
+    # writes 32 B of per-Gaussian records instead of keys)
+    pre_bytes = P * (12 + 4 + 24 + 96) + (P * 32 if df else num * 12)
     cand = {"k_pass": (pass_avg, pass_bytes), "k_preprocess": (stage_avg["preprocess"], pre_bytes)}
     dom = max(cand, key=lambda k: cand[k][0] * (len(working) if k == "k_pass" else 1))
     dur_ms, abytes = cand[dom]
@@ -353,13 +383,19 @@ def run_gsr(args):
             cpu = {"value": cfps, "unit": "frames/s", "cores": threads, "kind": "port",
                    "sample": "%d whole frames of %s in %.1f s (FP64 oracle, %d threads)" % (n, args.workload, el,
                                                                                           threads)}
-        # preprocess + massive emission + upsweep + digit passes + tile ranges + render
-        launches_per_frame = 2 + 1 + passes + 1 + 1
+        if df:
+            # counting pass + massive count, compact, depth sort (upsweep + 4),
+            # offsets, two emission kernels, tile sort, tile ranges, render
+            launches_per_frame = 2 + 1 + 5 + 1 + 2 + 1 + tile_passes + 1 + 1
+        else:
+            # preprocess + massive emission + upsweep + digit passes + tile ranges + render
+            launches_per_frame = 2 + 1 + passes + 1 + 1
         line = {"metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": world, "steps": K,
                 "warmup": max(3, args.warmup), "ms_per_step": elapsed_ms / K, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": args.workload, "gaussians": P, "width": cam.width, "height": cam.height,
                            "tile": "16x16", "variant": E2E_VARIANT, "sh": "fp16", "num_rendered": num,
+                           "pipeline": args.pipeline,
                            "sort_bits": end_bit, "sort_working_passes": len(working), "l2": "inputs larger than L2 (scene %.0f MB)" %
                            (scene.device_bytes() / 1e6), "parallelism": "replicas" if world > 1 else "single"},
                 "stages_ms": stage_avg, "roofline": roofline, "cpu_baseline": cpu, "reference_gpu": ref_gpu,

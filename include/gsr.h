@@ -162,6 +162,30 @@ gsr_status gsr_forward(int variant, int P, const float* pos, const void* shs, in
                        int64_t key_capacity, float* points_xy, float* rgb_depth, float* conic_opacity,
                        int32_t* ranges, const float* bg_color, uint8_t* out_color, gsr_stream_t stream);
 
+/* ---- depth-first forward ------------------------------------------------ */
+/* The reference's "early sorting" two-pass pipeline
+ * (csrc/cuda_rasterizer/preprocess.cu:673-1248, sort.cu:151-285,
+ * example.py:246-291) as one call: a counting pass, a depth sort of the
+ * Gaussians that hit a tile, emission of (tile, Gaussian) pairs in depth
+ * order, a stable sort of the 32-bit tile ids, tile ranges and the render.
+ * Same image as gsr_forward; pairs with equal tile and equal depth bits keep
+ * Gaussian index order.  `scene_scratch` holds gsr_depth_first_scratch_size(P)
+ * bytes of per-Gaussian arrays.  On return tiles_sorted / values_sorted hold
+ * the sorted pairs, `ranges` (or, when NULL, the workspace's range area) the
+ * tile ranges, and *curr_offset the pair count M (M > key_capacity:
+ * overflow, reported by gsr_read_status).  Any variant; ranges are always
+ * precomputed. */
+size_t gsr_depth_first_scratch_size(int P);
+gsr_status gsr_forward_depth_first(int variant, int P, const float* pos, const void* shs, int shs_half,
+                                   const float* opacity, const float* cov3d, int width, int height, int block_x,
+                                   int block_y, const float* cam_pos, const float* cam_rot, float focal_x,
+                                   float focal_y, float z_far, float z_near, int32_t* curr_offset, void* workspace,
+                                   size_t workspace_bytes, void* scene_scratch, size_t scene_scratch_bytes,
+                                   uint32_t* tiles_unsorted, uint32_t* values_unsorted, uint32_t* tiles_sorted,
+                                   uint32_t* values_sorted, int64_t key_capacity, float* points_xy, float* rgb_depth,
+                                   float* conic_opacity, int32_t* ranges, const float* bg_color, uint8_t* out_color,
+                                   gsr_stream_t stream);
+
 /* ---- stage timing ------------------------------------------------------- */
 /* Profiling hook with no counterpart in the reference.  After
  * gsr_profile_begin(frames), each of the next `frames` gsr_forward calls

@@ -172,19 +172,19 @@ gsr_status gsr_scene_prepare(int P, const float* log_scales, const float* quats,
     return from_cuda(launch_scene_prepare(P, log_scales, quats, opacity_logits, opacity, cov3d, (cudaStream_t)stream));
 }
 
-static gsr_status preprocess_impl(int P, const float* pos, const void* shs, int shs_half, const float* opacity,
-                                  const float* cov3d, int width, int height, int block_x, int block_y,
-                                  const float* cam_pos, const float* cam_rot, float fx, float fy, float zfar,
-                                  float znear, float* points_xy, float* rgb_depth, float* conic_opacity,
-                                  uint64_t* keys, uint32_t* values, int64_t cap, int32_t* curr_offset,
-                                  void* workspace, size_t workspace_bytes, cudaStream_t s)
+static gsr_status preprocess_params(PreprocessParams& p, int P, const float* pos, const void* shs,
+                                    const float* opacity, const float* cov3d, int width, int height, int block_x,
+                                    int block_y, const float* cam_pos, const float* cam_rot, float fx, float fy,
+                                    float zfar, float znear, float* points_xy, float* rgb_depth,
+                                    float* conic_opacity, uint64_t* keys, uint32_t* values, int64_t cap,
+                                    int32_t* curr_offset, void* workspace, size_t workspace_bytes)
 {
     if (P < 0 || width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0 || !cam_pos || !cam_rot || !curr_offset)
         return GSR_INVALID_ARG;
     if (P > 0 && (!pos || !shs || !opacity || !cov3d || !points_xy || !rgb_depth || !conic_opacity))
         return GSR_INVALID_ARG;
     if (cap > 0 && (!keys || !values)) return GSR_INVALID_ARG;
-    PreprocessParams p;
+    p.df = DepthFirstRecords{nullptr, nullptr, nullptr, nullptr};
     p.P = P;
     p.pos = pos;
     p.shs = shs;
@@ -211,17 +211,33 @@ static gsr_status preprocess_impl(int P, const float* pos, const void* shs, int 
     p.vals = values;
     p.cap = cap;
     p.counter = curr_offset;
-    p.mq.capacity = 0;
+    p.mq.capacity = p.mq.huge_capacity = 0;
     p.mq.entries = nullptr;
     p.mq.count = p.mq.head = p.mq.depth_hi = nullptr;
     if (workspace && workspace_bytes >= kSmallWorkspaceBytes) {
         WorkspaceHeader* h = reinterpret_cast<WorkspaceHeader*>(workspace);
         p.mq.entries = reinterpret_cast<MassiveEntry*>(reinterpret_cast<char*>(workspace) + kHeaderBytes);
         p.mq.capacity = kMassiveQueueEntries;
-        p.mq.count = &h->mq_count;
-        p.mq.head = &h->mq_head;
+        p.mq.huge_capacity = kMassiveHugeEntries;
+        p.mq.count = h->mq_count;
+        p.mq.head = &h->mq_head[0][0];
         p.mq.depth_hi = &h->depth_hi;
     }
+    return GSR_OK;
+}
+
+static gsr_status preprocess_impl(int P, const float* pos, const void* shs, int shs_half, const float* opacity,
+                                  const float* cov3d, int width, int height, int block_x, int block_y,
+                                  const float* cam_pos, const float* cam_rot, float fx, float fy, float zfar,
+                                  float znear, float* points_xy, float* rgb_depth, float* conic_opacity,
+                                  uint64_t* keys, uint32_t* values, int64_t cap, int32_t* curr_offset,
+                                  void* workspace, size_t workspace_bytes, cudaStream_t s)
+{
+    PreprocessParams p;
+    const gsr_status st = preprocess_params(p, P, pos, shs, opacity, cov3d, width, height, block_x, block_y, cam_pos,
+                                            cam_rot, fx, fy, zfar, znear, points_xy, rgb_depth, conic_opacity, keys,
+                                            values, cap, curr_offset, workspace, workspace_bytes);
+    if (st != GSR_OK) return st;
     return from_cuda(launch_preprocess(p, shs_half != 0, s));
 }
 
@@ -385,6 +401,54 @@ gsr_status gsr_forward(int variant, int P, const float* pos, const void* shs, in
     }
     st = render_impl(variant, 0, curr_offset, key_capacity, width, height, block_x, block_y, P, points_xy, rgb_depth,
                      conic_opacity, keys_sorted, values_sorted, ranges, bg_color, out_color, workspace, s);
+    if (st == GSR_OK) profile_mark(s);
+    return st;
+}
+
+size_t gsr_depth_first_scratch_size(int P) { return P < 0 ? 0 : df_scratch_bytes(P); }
+
+gsr_status gsr_forward_depth_first(int variant, int P, const float* pos, const void* shs, int shs_half,
+                                   const float* opacity, const float* cov3d, int width, int height, int block_x,
+                                   int block_y, const float* cam_pos, const float* cam_rot, float focal_x,
+                                   float focal_y, float z_far, float z_near, int32_t* curr_offset, void* workspace,
+                                   size_t workspace_bytes, void* scene_scratch, size_t scene_scratch_bytes,
+                                   uint32_t* tiles_unsorted, uint32_t* values_unsorted, uint32_t* tiles_sorted,
+                                   uint32_t* values_sorted, int64_t key_capacity, float* points_xy, float* rgb_depth,
+                                   float* conic_opacity, int32_t* ranges, const float* bg_color, uint8_t* out_color,
+                                   gsr_stream_t stream)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!workspace || !curr_offset || !scene_scratch || !valid_tile_shape(block_x, block_y)) return GSR_INVALID_ARG;
+    if (variant < 0 || variant > GSR_RENDER_DT) return GSR_INVALID_ARG;
+    if (workspace_bytes < sort_workspace_bytes(key_capacity) || key_capacity >= (1LL << 30)) return GSR_INVALID_ARG;
+    if (P < 0 || scene_scratch_bytes < df_scratch_bytes(P)) return GSR_INVALID_ARG;
+    if (key_capacity > 0 && (!tiles_unsorted || !values_unsorted || !tiles_sorted || !values_sorted))
+        return GSR_INVALID_ARG;
+    if (tiles_unsorted == tiles_sorted || values_unsorted == values_sorted) return GSR_INVALID_ARG;
+    const int tiles = tiles_of(width, height, block_x, block_y);
+    if (!ranges) {
+        if (tiles > kWorkspaceRangeTiles) return GSR_INVALID_ARG;
+        ranges = reinterpret_cast<int32_t*>(workspace_ranges(workspace, key_capacity));
+    }
+    PreprocessParams p;
+    // the counting pass emits no 64-bit keys: the key pointers only pass the checks
+    gsr_status st = preprocess_params(p, P, pos, shs, opacity, cov3d, width, height, block_x, block_y, cam_pos, cam_rot,
+                                      focal_x, focal_y, z_far, z_near, points_xy, rgb_depth, conic_opacity,
+                                      reinterpret_cast<uint64_t*>(tiles_unsorted), values_unsorted, key_capacity,
+                                      curr_offset, workspace, workspace_bytes);
+    if (st != GSR_OK) return st;
+    profile_frame_begin();
+    cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(uint32_t), s);  // status word
+    if (e == cudaSuccess) e = cudaMemsetAsync(curr_offset, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess) return from_cuda(e);
+    profile_mark(s);
+    e = launch_depth_first(p, shs_half != 0, scene_scratch, scene_scratch_bytes,
+                           reinterpret_cast<WorkspaceHeader*>(workspace), workspace_sort_scratch(workspace, key_capacity),
+                           tiles, tiles_unsorted, values_unsorted, tiles_sorted, values_sorted,
+                           reinterpret_cast<int2*>(ranges), s);
+    if (e != cudaSuccess) return from_cuda(e);
+    st = render_impl(variant, 0, curr_offset, key_capacity, width, height, block_x, block_y, P, points_xy, rgb_depth,
+                     conic_opacity, nullptr, values_sorted, ranges, bg_color, out_color, workspace, s);
     if (st == GSR_OK) profile_mark(s);
     return st;
 }

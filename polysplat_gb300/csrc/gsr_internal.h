@@ -1,6 +1,8 @@
 // Internal launch interfaces shared between the gsr translation units.
 #pragma once
 
+#include <cstddef>
+
 #include "gsr_common.cuh"
 
 namespace gsr {
@@ -13,16 +15,32 @@ struct MassiveEntry {
     int4 rect;               // tile rectangle [x0, x1) x [y0, y1)
 };
 
+// Two classes share one array: slots [0, huge_capacity) hold "huge"
+// rectangles (swept by a whole CTA), the rest "large" ones (one warp each).
+// A huge rectangle that finds its region full goes to the large region (a
+// warp handles any size, only more slowly); one that finds both full is
+// handled in place by its own warp in the preprocess.
 struct MassiveQueue {
     MassiveEntry* entries;
-    int capacity;
-    uint32_t* count;     // entries pushed (may exceed capacity: the rest were handled in place)
-    uint32_t* head;      // entries taken by the second kernel
+    int capacity;        // total slots
+    int huge_capacity;   // slots of the huge region
+    uint32_t* count;     // [2] entries pushed: huge, large (may exceed the region: the rest went elsewhere)
+    uint32_t* head;      // [2][2] entries taken: [pass][class]; pass 0 counts or emits keys, pass 1
+                         // emits the depth-first pairs
     uint32_t* depth_hi;  // max depth bits of emitting Gaussians (for the sort's key compression)
+};
+
+// Per-Gaussian records of the depth-first pipeline's counting pass.
+struct DepthFirstRecords {
+    uint32_t* count;  // [P] number of tiles the Gaussian's keys go to
+    uint32_t* dkey;   // [P] depth bit pattern (the key's low word)
+    float4* geo;      // [P] conic x, y, z and power (the exact FP32 test inputs)
+    int2* rect;       // [P] x0 | x1 << 16, y0 | y1 << 16; bit 31 of .y: queued as massive
 };
 
 struct PreprocessParams {
     MassiveQueue mq;
+    DepthFirstRecords df;  // count mode only
     int P;
     const float* pos;
     const void* shs;
@@ -45,6 +63,15 @@ struct PreprocessParams {
 void camera_matrices(int W, int H, const float* pos, const float* rot, float fx, float fy, float zfar, float znear,
                      float* view, float* proj);
 cudaError_t launch_preprocess(const PreprocessParams& p, bool half_sh, cudaStream_t stream);
+// Depth-first pipeline: counting pass (fills p.df, features and the massive
+// queue), then the emission of a Gaussian's pairs at its offset (small
+// rectangles and queued Gaussians separately).
+cudaError_t launch_preprocess_count(const PreprocessParams& p, bool half_sh, cudaStream_t stream);
+cudaError_t launch_df_emit_small(const PreprocessParams& p, const uint32_t* d_v, const uint32_t* sgids,
+                                 const uint32_t* offsets, uint32_t* tiles, uint32_t* vals, long long cap,
+                                 cudaStream_t stream);
+cudaError_t launch_df_emit_massive(const PreprocessParams& p, const uint32_t* offsets, const uint32_t* rank,
+                                   uint32_t* tiles, uint32_t* vals, long long cap, cudaStream_t stream);
 cudaError_t launch_scene_prepare(int P, const float* log_scales, const float* quats, const float* logits,
                                  float* opacity, float* cov3d, cudaStream_t stream);
 
@@ -56,22 +83,29 @@ struct WorkspaceHeader {
     uint32_t status;          // OR of kErr* bits
     uint32_t render_queue;    // persistent render tile counter
     // preprocess region (cleared by every preprocess)
-    uint32_t mq_count;        // massive-Gaussian queue: entries pushed
-    uint32_t mq_head;         // massive-Gaussian queue: entries taken
+    uint32_t mq_count[2];     // massive-Gaussian queue: entries pushed per class
+    uint32_t mq_head[2][2];   // massive-Gaussian queue: entries taken per pass and class
     uint32_t depth_hi;        // largest depth bit pattern of an emitting Gaussian
-    uint32_t pad[3];
+    uint32_t pad[7];
     // sort region (cleared by every sort)
     uint32_t pass_counter[8]; // per radix pass tile counter
     uint32_t hist[8][256];    // per-pass digit histograms
 };
-constexpr size_t kSortRegionOffset = 8 * sizeof(uint32_t);
+constexpr size_t kPreprocessRegionOffset = 2 * sizeof(uint32_t);
+constexpr size_t kPreprocessRegionBytes = 7 * sizeof(uint32_t);
+constexpr size_t kSortRegionOffset = 16 * sizeof(uint32_t);
 constexpr size_t kHeaderBytes = 16384;
 static_assert(sizeof(WorkspaceHeader) <= kHeaderBytes, "header too large");
+static_assert(offsetof(WorkspaceHeader, mq_count) == kPreprocessRegionOffset &&
+                  offsetof(WorkspaceHeader, pad) == kPreprocessRegionOffset + kPreprocessRegionBytes &&
+                  offsetof(WorkspaceHeader, pass_counter) == kSortRegionOffset,
+              "header layout");
 
 // Massive-Gaussian queue capacity of a workspace (entries of 48 bytes); the
 // queue sits right after the header.  Gaussians beyond it are emitted in
 // place by their own warp (slower, same keys).
 constexpr int kMassiveQueueEntries = 1 << 18;
+constexpr int kMassiveHugeEntries = 1 << 15;
 constexpr size_t kMassiveQueueBytes = (size_t)kMassiveQueueEntries * sizeof(MassiveEntry);
 // Small workspace for preprocess-only and render-only calls.
 constexpr size_t kSmallWorkspaceBytes = kHeaderBytes + kMassiveQueueBytes;
@@ -111,8 +145,35 @@ struct SortArgs {
 };
 cudaError_t launch_sort(const SortArgs& a, cudaStream_t stream);
 
+// Generic sort plumbing (also used by the depth-first pipeline).
+enum : int {
+    kOrderMasked = 0,             // key & mask(end_bit)
+    kOrderDepthCompressed64 = 1,  // (tile << nb) | (low word - floor), nb from the header's depth_hi
+    kOrderDepth32 = 2,            // 32-bit depth bits - floor, width from the header's depth_hi
+};
+struct OrderMap {
+    int kind;
+    int end_bit;
+};
+struct SortScratch {
+    WorkspaceHeader* hdr;  // counters, histograms, status, depth_hi
+    void* alt_keys;
+    uint32_t* alt_vals;
+    uint32_t* look[2];
+    long long tiles_cap;
+};
+size_t sort_scratch_bytes(long long cap, int key_bytes);
+SortScratch carve_sort_scratch(WorkspaceHeader* hdr, void* mem, long long cap, int key_bytes);
+SortScratch workspace_sort_scratch(void* ws, long long cap);
+cudaError_t launch_sort32(int num, const int32_t* d_num, long long cap, OrderMap order, int max_passes,
+                          const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                          const SortScratch& s, cudaStream_t stream);
+
 cudaError_t launch_tile_ranges(int num, const int32_t* d_num, long long cap, int tiles, const uint64_t* keys,
                                int32_t* ranges, bool scan_semantics, cudaStream_t stream);
+// Same, over sorted 32-bit tile ids.
+cudaError_t launch_tile_ranges32(const int32_t* d_num, long long cap, int tiles, const uint32_t* tile_ids,
+                                 int2* ranges, cudaStream_t stream);
 cudaError_t launch_gather(int num, const int32_t* d_num, const uint32_t* values, const float2* sxy,
                           const float4* srgbd, const float4* scon, float2* dxy, float4* drgbd, float4* dcon,
                           long long cap, cudaStream_t stream);
@@ -135,6 +196,15 @@ struct RenderArgs {
     WorkspaceHeader* ws;
 };
 cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream);
+
+// Depth-first forward (depthfirst.cu): scratch of P-sized arrays, and the
+// pipeline from the counting pass to the tile ranges.  The emitted pair count
+// goes to p.counter; tile ids and values land in tile_keys_out / vals_out.
+size_t df_scratch_bytes(int P);
+cudaError_t launch_depth_first(const PreprocessParams& p, bool half_sh, void* scratch, size_t scratch_bytes,
+                               WorkspaceHeader* hdr, const SortScratch& tile_sort, int tiles, uint32_t* tile_keys_in,
+                               uint32_t* vals_in, uint32_t* tile_keys_out, uint32_t* vals_out, int2* ranges,
+                               cudaStream_t stream);
 
 int device_sm_count();
 

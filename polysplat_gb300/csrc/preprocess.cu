@@ -9,6 +9,8 @@
 // library's own: 8 warps per CTA, each warp owns 32 consecutive Gaussians,
 // and keys are staged per warp in shared memory and flushed with one global
 // atomic per flush instead of one per 32-wide emission step.
+#include <algorithm>
+
 #include "gsr_internal.h"
 
 namespace gsr {
@@ -266,6 +268,8 @@ __device__ __forceinline__ void stage_emit(Stage& s, const EmitOut& o, bool vali
 
 // Tile rectangles at least this large are queued for k_emit_massive.
 constexpr int kMassiveArea = 32;
+// Rectangles of at least this many tiles are swept by a whole CTA.
+constexpr int kHugeArea = 2048;
 
 // Block-wide final flush of every warp's staged keys with one atomic per CTA.
 __device__ __forceinline__ void block_flush(Stage& st, const EmitOut& out, int* s_fill, long long* s_base,
@@ -299,15 +303,20 @@ __device__ __forceinline__ void block_flush(Stage& st, const EmitOut& out, int* 
     st.fill = 0;
 }
 
-template <bool HALF>
+// COUNT = false: emit (tile | depth, index) keys (the reference's single-pass
+// pipeline).  COUNT = true: the depth-first pipeline's counting pass -- the
+// same tests, but each Gaussian's number of hit tiles is counted and written
+// with its depth and test geometry instead of keys.
+template <bool HALF, bool COUNT>
 __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessParams a)
 {
-    __shared__ uint64_t s_keys[kWarps][kStage];
-    __shared__ uint32_t s_vals[kWarps][kStage];
+    __shared__ uint64_t s_keys[COUNT ? 1 : kWarps][kStage];
+    __shared__ uint32_t s_vals[COUNT ? 1 : kWarps][kStage];
     __shared__ int s_fill[kWarps];
     __shared__ long long s_base[kWarps];
     __shared__ uint32_t s_hit[kWarps];
     __shared__ int s_pref[kWarps][32];
+    __shared__ uint32_t s_cnt[kWarps][32];
 
     const unsigned lane = threadIdx.x & 31u;
     const int warp = threadIdx.x >> 5;
@@ -358,19 +367,26 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
         } while (false);
     }
 
-    Stage st{s_keys[warp], s_vals[warp], 0};
+    Stage st{s_keys[COUNT ? 0 : warp], s_vals[COUNT ? 0 : warp], 0};
     const EmitOut out{a.keys, a.vals, a.cap, a.counter};
     if (lane == 0) s_hit[warp] = 0u;
+    s_cnt[warp][lane] = 0u;
     __syncwarp();
     const uint32_t depth_bits = __float_as_uint(p_view.z);
+    const bool was_valid = point_valid;
+    bool queued = false;
 
     // (1) single-tile Gaussians: one test per thread.
     const int area = (rect_max.x - rect_min.x) * (rect_max.y - rect_min.y);
     const bool single = point_valid && area == 1;
     {
         bool v = single && tile_hit(rect_min.x, rect_min.y, a.bx, a.by, point_xy, conic, power);
-        uint64_t key = ((uint64_t)(uint32_t)(rect_min.y * gridx + rect_min.x) << 32) | depth_bits;
-        stage_emit(st, out, v, key, (uint32_t)idx, lane);
+        if (COUNT) {
+            if (v) s_cnt[warp][lane] = 1u;
+        } else {
+            uint64_t key = ((uint64_t)(uint32_t)(rect_min.y * gridx + rect_min.x) << 32) | depth_bits;
+            stage_emit(st, out, v, key, (uint32_t)idx, lane);
+        }
         unsigned m = __ballot_sync(GSR_FULL_MASK, v);
         if (lane == 0 && m) atomicOr(&s_hit[warp], m);
     }
@@ -385,24 +401,36 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
     // tile of the rectangle with the same test, so the key set is the same.
     bool massive = point_valid && area >= kMassiveArea;
     {
-        const unsigned mm = __ballot_sync(GSR_FULL_MASK, massive);
-        int qbase = 0;
-        if (mm) {
-            if (lane == 0) qbase = (int)atomicAdd(a.mq.count, (uint32_t)__popc(mm));
-            qbase = __shfl_sync(GSR_FULL_MASK, qbase, 0);
+        // huge rectangles first try the CTA-swept region, then the warp one
+        int slot = -1;
+        const bool want_huge = massive && area >= kHugeArea;
+        const unsigned mh = __ballot_sync(GSR_FULL_MASK, want_huge);
+        if (mh) {
+            int base = 0;
+            if (lane == 0) base = (int)atomicAdd(&a.mq.count[0], (uint32_t)__popc(mh));
+            base = __shfl_sync(GSR_FULL_MASK, base, 0);
+            const int s0 = base + __popc(mh & lanemask_lt());
+            if (want_huge && s0 < a.mq.huge_capacity) slot = s0;
         }
-        if (massive) {
-            const int slot = qbase + __popc(mm & lanemask_lt());
-            if (slot < a.mq.capacity) {
-                MassiveEntry e;
-                e.ctr_power_depth = make_float4(point_xy.x, point_xy.y, power, p_view.z);
-                e.conic_gid = make_float4(conic.x, conic.y, conic.z, __uint_as_float((uint32_t)idx));
-                e.rect = make_int4(rect_min.x, rect_max.x, rect_min.y, rect_max.y);
-                a.mq.entries[slot] = e;
-                atomicOr(&s_hit[warp], 1u << lane);  // features are written for queued Gaussians
-                point_valid = false;
-                massive = false;
-            }
+        const bool want_large = massive && slot < 0;
+        const unsigned ml = __ballot_sync(GSR_FULL_MASK, want_large);
+        if (ml) {
+            int base = 0;
+            if (lane == 0) base = (int)atomicAdd(&a.mq.count[1], (uint32_t)__popc(ml));
+            base = __shfl_sync(GSR_FULL_MASK, base, 0);
+            const int s1 = base + __popc(ml & lanemask_lt());
+            if (want_large && s1 < a.mq.capacity - a.mq.huge_capacity) slot = a.mq.huge_capacity + s1;
+        }
+        if (slot >= 0) {
+            MassiveEntry e;
+            e.ctr_power_depth = make_float4(point_xy.x, point_xy.y, power, p_view.z);
+            e.conic_gid = make_float4(conic.x, conic.y, conic.z, __uint_as_float((uint32_t)idx));
+            e.rect = make_int4(rect_min.x, rect_max.x, rect_min.y, rect_max.y);
+            a.mq.entries[slot] = e;
+            atomicOr(&s_hit[warp], 1u << lane);  // features are written for queued Gaussians
+            point_valid = false;
+            massive = false;
+            queued = true;
         }
     }
     // queue overflow: the warp runs the Gaussian's whole rectangle itself
@@ -423,8 +451,13 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
             for (int x0 = x_lo; x0 < x_hi; x0 += 8) {
                 const int x = x0 + tx;
                 bool v = y < y_hi && x < x_hi && tile_hit(x, y, a.bx, a.by, c, q, pw);
-                uint64_t key = ((uint64_t)(uint32_t)(y * gridx + x) << 32) | db;
-                stage_emit(st, out, v, key, gid, lane);
+                if (COUNT) {
+                    const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
+                    if (lane == 0) s_cnt[warp][i] += __popc(m);
+                } else {
+                    uint64_t key = ((uint64_t)(uint32_t)(y * gridx + x) << 32) | db;
+                    stage_emit(st, out, v, key, gid, lane);
+                }
             }
         }
         if (lane == 0) atomicOr(&s_hit[warp], 1u << i);
@@ -475,8 +508,12 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
                 y = oy + row;
                 v = tile_hit(x, y, a.bx, a.by, c, q, pw);
             }
-            uint64_t key = ((uint64_t)(uint32_t)(y * gridx + x) << 32) | db;
-            stage_emit(st, out, v, key, (uint32_t)(warp_first + owner), lane);
+            if (COUNT) {
+                if (v) atomicAdd(&s_cnt[warp][owner], 1u);
+            } else {
+                uint64_t key = ((uint64_t)(uint32_t)(y * gridx + x) << 32) | db;
+                stage_emit(st, out, v, key, (uint32_t)(warp_first + owner), lane);
+            }
             if (v) atomicOr(&s_hit[warp], 1u << owner);
         }
     }
@@ -497,146 +534,359 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
         a.rgb_depth[idx] = make_float4(col.x, col.y, col.z, p_view.z);
     }
 
-    // (4) block-wide final flush: one atomic per CTA.
-    block_flush(st, out, s_fill, s_base, lane, warp);
+    if (COUNT) {
+        // (4') records of the counting pass (queued Gaussians get their count
+        // from the massive kernel, which runs next)
+        if (idx < a.P) {
+            a.df.count[idx] = was_valid ? s_cnt[warp][lane] : 0u;
+            if (was_valid) {
+                a.df.dkey[idx] = depth_bits;
+                a.df.geo[idx] = make_float4(conic.x, conic.y, conic.z, power);
+                a.df.rect[idx] = make_int2((int)((uint32_t)rect_min.x | ((uint32_t)rect_max.x << 16)),
+                                           (int)((uint32_t)rect_min.y | ((uint32_t)rect_max.y << 16) |
+                                                 (queued ? 0x80000000u : 0u)));
+            }
+        }
+    } else {
+        // (4) block-wide final flush: one atomic per CTA.
+        block_flush(st, out, s_fill, s_base, lane, warp);
+    }
 }
 
 // ---------------------------------------------------------------------------
-// Queued Gaussians with large tile rectangles: persistent CTAs take one
-// Gaussian at a time and all 256 threads test its tiles, 256 per step, so a
-// screen-filling Gaussian costs ~32 steps of one CTA instead of ~255 steps of
-// one warp that also holds up its own CTA.
-constexpr int kMaxBandRows = 1024;  // tile rows of a rectangle that get candidate bands
+// Queued Gaussians with large tile rectangles (k_emit_massive).  For a
+// well-conditioned ellipse only the tiles of each tile row that lie within a
+// margin of the ellipse's x-extent over that row get the exact test; tiles
+// farther out cannot pass it.
+constexpr int kMaxBandRows = 1024;  // tile rows of a CTA-swept rectangle that get candidate bands
 
-// Per-Gaussian constants of the ellipse A dx^2 + 2B dx dy + C dy^2 <= w,
-// derived in double from the FP32 conic (det = AC - B^2 is where cancellation
-// would hurt), then used in float per tile row.
+// Ellipse A dx^2 + 2B dx dy + C dy^2 <= w (w = 2 power) in float.  det = AC - B^2
+// is formed with a single rounding (Kahan's fused difference of products),
+// and the half-width at height dy as sqrt(det (dymax - dy)(dymax + dy)) / A,
+// which does not cancel near the top and bottom, so every extent carries a
+// few ulp of relative error: well under a pixel while the extents stay below
+// 1e6 px, against a margin of two tiles.  Ill-conditioned ellipses
+// (det <= 1e-6 AC), where the exact test itself is at the mercy of
+// cancellation, and non-finite values get every tile of the rectangle tested.
 struct Band {
-    float A, B, Aw, det, dymax, dxmax, dyr, cx, cy, m;
+    float B, inv_a, det, dymax, dxmax, dyr, cx, cy, m;
+    bool ok;
 };
 
-__device__ __forceinline__ Band make_band(double A, double B, double C, double w, double det, float cx, float cy,
-                                          float m)
+__device__ __forceinline__ Band make_band(float3 q, float power, float2 c, float m)
 {
     Band b;
-    b.A = (float)A;
-    b.B = (float)B;
-    b.Aw = (float)(A * w);
-    b.det = (float)det;
-    b.dymax = (float)sqrt(w * A / det);
-    b.dxmax = (float)sqrt(w * C / det);
-    b.dyr = (float)(-B * sqrt(w / (C * det)));  // dy where the ellipse reaches its largest x
-    b.cx = cx;
-    b.cy = cy;
+    const float A = q.x, B = q.y, C = q.z, w = 2.0f * power;
+    const float bb = B * B;
+    const float det = fmaf(A, C, -bb) + fmaf(-B, B, bb);
+    b.B = B;
+    b.inv_a = 1.0f / A;
+    b.det = det;
+    b.dymax = sqrtf(w * A / det);
+    b.dxmax = sqrtf(w * C / det);
+    b.dyr = -B * sqrtf(w / (C * det));  // dy where the ellipse reaches its largest x
+    b.cx = c.x;
+    b.cy = c.y;
     b.m = m;
+    b.ok = A > 0.0f && C > 0.0f && w > 0.0f && det > 1e-6f * (A * C) && b.dymax < 1e6f && b.dxmax < 1e6f &&
+           fabsf(b.dyr) < 1e6f && fabsf(c.x) < 1e7f && fabsf(c.y) < 1e7f;
     return b;
 }
 
-// Candidate tile columns of tile row `ty`: the ellipse's x-extent over the
-// row's pixel band, widened by m pixels on every side.  False when the
-// widened band misses the ellipse.
+// Candidate tile columns [c_lo, c_hi] of tile row `ty`: the ellipse's x-extent
+// over the row's pixel band, widened by m pixels on every side.  False when
+// the widened band misses the ellipse.
 __device__ __forceinline__ bool band_columns(const Band& e, int ty, int by, int bx, int x_lo, int x_hi, int& c_lo,
                                              int& c_hi)
 {
     const float p = fmaxf((float)(ty * by) - e.m - e.cy, -e.dymax);
     const float q = fminf((float)(ty * by + by - 1) + e.m - e.cy, e.dymax);
-    if (p > q) return false;
-    auto half = [&](float dy) { return sqrtf(fmaxf(0.0f, e.Aw - e.det * dy * dy)); };
+    if (!(p <= q)) return false;
+    auto half = [&](float dy) {
+        return sqrtf(e.det * fmaxf(0.0f, e.dymax - dy) * fmaxf(0.0f, e.dymax + dy)) * e.inv_a;
+    };
     const float hp = half(p), hq = half(q);
-    const float xr = (e.dyr >= p && e.dyr <= q) ? e.dxmax : fmaxf((-e.B * p + hp) / e.A, (-e.B * q + hq) / e.A);
-    const float xl = (-e.dyr >= p && -e.dyr <= q) ? -e.dxmax : fminf((-e.B * p - hp) / e.A, (-e.B * q - hq) / e.A);
+    const float mp = -e.B * p * e.inv_a, mq = -e.B * q * e.inv_a;  // centre line of the ellipse at p, q
+    const float xr = (e.dyr >= p && e.dyr <= q) ? e.dxmax : fmaxf(mp + hp, mq + hq);
+    const float xl = (-e.dyr >= p && -e.dyr <= q) ? -e.dxmax : fminf(mp - hp, mq - hq);
     const float lo = floorf((e.cx + xl - e.m) / (float)bx), hi = floorf((e.cx + xr + e.m) / (float)bx);
     c_lo = (int)fmaxf((float)x_lo, lo);
     c_hi = (int)fminf((float)(x_hi - 1), hi);
     return c_lo <= c_hi;
 }
 
-__global__ __launch_bounds__(kThreads) void k_emit_massive(const PreprocessParams a)
+// Sweep the tiles of one huge queued Gaussian with the whole CTA; on_step(v,
+// x, y) is called by every lane of a warp together, v = the tile's exact test.
+template <typename F>
+__device__ __forceinline__ void sweep_cta(const MassiveEntry& me, const PreprocessParams& a, short2* s_band,
+                                          unsigned lane, int warp, F&& on_step)
 {
-    __shared__ uint64_t s_keys[kWarps][kStage];
-    __shared__ uint32_t s_vals[kWarps][kStage];
+    const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
+    const float pw = me.ctr_power_depth.z;
+    const float3 q = {me.conic_gid.x, me.conic_gid.y, me.conic_gid.z};
+    const int x_lo = me.rect.x, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
+    const int w = x_hi - x_lo;
+    // every thread forms the same band from the same inputs: a uniform branch
+    const Band eb = make_band(q, pw, c, 2.0f * (float)max(a.bx, a.by));
+    if (eb.ok && (y_hi - y_lo) <= kMaxBandRows) {
+        for (int r = threadIdx.x; r < y_hi - y_lo; r += kThreads) {
+            int clo = 0, chi = -1;
+            if (!band_columns(eb, y_lo + r, a.by, a.bx, x_lo, x_hi, clo, chi)) {
+                clo = 0;
+                chi = -1;
+            }
+            s_band[r] = make_short2((short)clo, (short)chi);
+        }
+        __syncthreads();
+        for (int r = warp; r < y_hi - y_lo; r += kWarps) {
+            const short2 band = s_band[r];
+            const int y = y_lo + r;
+            for (int x0 = band.x; x0 <= band.y; x0 += 32) {
+                const int x = x0 + (int)lane;
+                const bool v = x <= band.y && tile_hit(x, y, a.bx, a.by, c, q, pw);
+                on_step(v, x, y);
+            }
+        }
+        __syncthreads();  // s_band and on_step's shared counters are reused by the next entry
+        return;
+    }
+    // Otherwise the CTA sweeps the rectangle in windows of (cols x rows)
+    // tiles, cols a power of two fitted to the rectangle's width, so narrow
+    // rectangles still fill the lanes and no per-tile integer division is
+    // needed.
+    int lg = 5;
+    while (lg > 0 && (1 << (lg - 1)) >= w) lg--;
+    const int cols = 1 << lg;              // columns per warp row
+    const int rows_w = 32 >> lg;           // rows per warp
+    const int rows_cta = rows_w * kWarps;  // rows per CTA step
+    const int lx = (int)lane & (cols - 1);
+    const int ly = warp * rows_w + ((int)lane >> lg);
+    for (int wy = y_lo; wy < y_hi; wy += rows_cta) {
+        const int y = wy + ly;
+        for (int wx = x_lo; wx < x_hi; wx += cols) {
+            const int x = wx + lx;
+            const bool v = y < y_hi && x < x_hi && tile_hit(x, y, a.bx, a.by, c, q, pw);
+            on_step(v, x, y);
+        }
+    }
+    __syncthreads();  // on_step's shared counters are reused by the next entry
+}
+
+// Sweep the tiles of one large queued Gaussian with one warp: the candidate
+// tiles of 32 rows at a time form one flattened task list, 32 tests per step.
+template <typename F>
+__device__ __forceinline__ void sweep_warp(const MassiveEntry& me, const PreprocessParams& a, unsigned lane,
+                                           F&& on_step)
+{
+    const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
+    const float pw = me.ctr_power_depth.z;
+    const float3 q = {me.conic_gid.x, me.conic_gid.y, me.conic_gid.z};
+    const int x_lo = me.rect.x, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
+    const Band eb = make_band(q, pw, c, 2.0f * (float)max(a.bx, a.by));
+    if (eb.ok) {
+        for (int r0 = y_lo; r0 < y_hi; r0 += 32) {
+            const int y = r0 + (int)lane;
+            int clo = 0, n = 0;
+            if (y < y_hi) {
+                int chi = -1;
+                if (band_columns(eb, y, a.by, a.bx, x_lo, x_hi, clo, chi)) n = chi - clo + 1;
+            }
+            int pref = n;  // inclusive prefix of the candidate counts
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int t = __shfl_up_sync(GSR_FULL_MASK, pref, d);
+                if ((int)lane >= d) pref += t;
+            }
+            const int total = __shfl_sync(GSR_FULL_MASK, pref, 31);
+            for (int base = 0; base < total; base += 32) {
+                const int task = base + (int)lane;
+                // owner row = first lane whose inclusive prefix exceeds the task
+                int lo = 0, hi = 31;
+#pragma unroll
+                for (int step = 0; step < 5; step++) {
+                    const int mid = (lo + hi) >> 1;
+                    if (__shfl_sync(GSR_FULL_MASK, pref, mid) > task) hi = mid;
+                    else lo = mid + 1;
+                }
+                const int o_pref = __shfl_sync(GSR_FULL_MASK, pref, lo);
+                const int o_n = __shfl_sync(GSR_FULL_MASK, n, lo);
+                const int o_clo = __shfl_sync(GSR_FULL_MASK, clo, lo);
+                const int x = o_clo + task - (o_pref - o_n);
+                const int yy = r0 + lo;
+                const bool v = task < total && tile_hit(x, yy, a.bx, a.by, c, q, pw);
+                on_step(v, x, yy);
+            }
+        }
+        return;
+    }
+    const int w = x_hi - x_lo;
+    const long long total = (long long)w * (long long)(y_hi - y_lo);
+    for (long long base = 0; base < total; base += 32) {
+        const long long t = base + lane;
+        int x = 0, y = 0;
+        bool v = false;
+        if (t < total) {
+            const int r = (int)(t / w);
+            y = y_lo + r;
+            x = x_lo + (int)(t - (long long)r * w);
+            v = tile_hit(x, y, a.bx, a.by, c, q, pw);
+        }
+        on_step(v, x, y);
+    }
+}
+
+// Where the depth-first pipeline's emission pass writes a queued Gaussian.
+struct DfEmit {
+    const uint32_t* offsets;  // [V] first output position of the s-th Gaussian in depth order
+    const uint32_t* rank;     // [P] depth-order position of Gaussian g
+    uint32_t* tiles;          // [cap] tile ids, depth-ordered per Gaussian
+    uint32_t* vals;           // [cap] Gaussian ids
+    long long cap;
+};
+
+enum : int { kMassiveEmit64 = 0, kMassiveCount = 1, kMassiveEmitDf = 2 };
+
+// Queued Gaussians: persistent CTAs first take the huge rectangles one at a
+// time with all 256 threads, then each warp takes large rectangles on its
+// own.  MODE: emit 64-bit keys, count the hit tiles (depth-first counting
+// pass), or write depth-first pairs at the Gaussian's offset.
+template <int MODE>
+__global__ __launch_bounds__(kThreads) void k_emit_massive(const PreprocessParams a, const DfEmit df)
+{
+    __shared__ uint64_t s_keys[MODE == kMassiveEmit64 ? kWarps : 1][kStage];
+    __shared__ uint32_t s_vals[MODE == kMassiveEmit64 ? kWarps : 1][kStage];
     __shared__ int s_fill[kWarps];
     __shared__ long long s_base[kWarps];
     __shared__ int s_entry;
+    __shared__ uint32_t s_pos;
+    __shared__ uint32_t s_wcnt[kWarps];
     __shared__ short2 s_band[kMaxBandRows];
     const unsigned lane = threadIdx.x & 31u;
     const int warp = threadIdx.x >> 5;
-    Stage st{s_keys[warp], s_vals[warp], 0};
+    Stage st{s_keys[MODE == kMassiveEmit64 ? warp : 0], s_vals[MODE == kMassiveEmit64 ? warp : 0], 0};
     const EmitOut out{a.keys, a.vals, a.cap, a.counter};
-    const int count = (int)min(*a.mq.count, (uint32_t)a.mq.capacity);
+    uint32_t* head = a.mq.head + (MODE == kMassiveEmitDf ? 2 : 0);
+    const int n_huge = (int)min(a.mq.count[0], (uint32_t)a.mq.huge_capacity);
+    const int n_large = (int)min(a.mq.count[1], (uint32_t)(a.mq.capacity - a.mq.huge_capacity));
+
+    // (1) huge rectangles, one CTA each
     for (;;) {
-        if (threadIdx.x == 0) s_entry = (int)atomicAdd(a.mq.head, 1u);
+        if (threadIdx.x == 0) {
+            s_entry = (int)atomicAdd(&head[0], 1u);
+            s_pos = 0u;
+        }
         __syncthreads();
         const int e = s_entry;
         __syncthreads();
-        if (e >= count) break;
+        if (e >= n_huge) break;
         const MassiveEntry me = a.mq.entries[e];
-        const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
-        const float pw = me.ctr_power_depth.z;
         const uint32_t db = __float_as_uint(me.ctr_power_depth.w);
-        const float3 q = {me.conic_gid.x, me.conic_gid.y, me.conic_gid.z};
         const uint32_t gid = __float_as_uint(me.conic_gid.w);
-        const int x_lo = me.rect.x, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
-        const int w = x_hi - x_lo;
-
-        // Well-conditioned ellipses: only tiles within two tiles of the
-        // ellipse's exact extent in each tile row get the (exact, FP32) test;
-        // tiles farther out cannot pass it.  The float evaluation error of the
-        // test stays far below that margin while det/(AC) > 1e-6 (worst case a
-        // few pixels at 8K); below that, or for non-finite values, every tile
-        // of the rectangle is tested.
-        const double A = q.x, B = q.y, C = q.z, W2 = 2.0 * (double)pw;
-        const double det = A * C - B * B;
-        const bool banded = (y_hi - y_lo) <= kMaxBandRows && A > 0.0 && C > 0.0 && W2 > 0.0 &&
-                            det > 1e-6 * A * C && isfinite(det) && isfinite(W2) && isfinite((double)c.x) &&
-                            isfinite((double)c.y);
-        if (banded) {
-            const Band eb = make_band(A, B, C, W2, det, c.x, c.y, 2.0f * (float)max(a.bx, a.by));
-            for (int r = threadIdx.x; r < y_hi - y_lo; r += kThreads) {
-                int clo = 0, chi = -1;
-                if (!band_columns(eb, y_lo + r, a.by, a.bx, x_lo, x_hi, clo, chi)) {
-                    clo = 0;
-                    chi = -1;
-                }
-                s_band[r] = make_short2((short)clo, (short)chi);
-            }
-            __syncthreads();
-            for (int r = warp; r < y_hi - y_lo; r += kWarps) {
-                const short2 band = s_band[r];
-                const int y = y_lo + r;
-                for (int x0 = band.x; x0 <= band.y; x0 += 32) {
-                    const int x = x0 + (int)lane;
-                    const bool v = x <= band.y && tile_hit(x, y, a.bx, a.by, c, q, pw);
-                    uint64_t key = ((uint64_t)(uint32_t)(y * a.gx + x) << 32) | db;
-                    stage_emit(st, out, v, key, gid, lane);
-                }
-            }
-            __syncthreads();  // s_band is rewritten by the next entry
-            continue;
-        }
-
-        // Otherwise the CTA sweeps the rectangle in windows of (cols x rows)
-        // tiles, cols a power of two fitted to the rectangle's width, so narrow
-        // rectangles still fill the lanes and no per-tile integer division is
-        // needed.
-        int lg = 5;
-        while (lg > 0 && (1 << (lg - 1)) >= w) lg--;
-        const int cols = 1 << lg;                // columns per warp row
-        const int rows_w = 32 >> lg;             // rows per warp
-        const int rows_cta = rows_w * kWarps;    // rows per CTA step
-        const int lx = (int)lane & (cols - 1);
-        const int ly = warp * rows_w + ((int)lane >> lg);
-        for (int wy = y_lo; wy < y_hi; wy += rows_cta) {
-            const int y = wy + ly;
-            for (int wx = x_lo; wx < x_hi; wx += cols) {
-                const int x = wx + lx;
-                const bool v = y < y_hi && x < x_hi && tile_hit(x, y, a.bx, a.by, c, q, pw);
+        if (MODE == kMassiveEmit64) {
+            sweep_cta(me, a, s_band, lane, warp, [&](bool v, int x, int y) {
                 uint64_t key = ((uint64_t)(uint32_t)(y * a.gx + x) << 32) | db;
                 stage_emit(st, out, v, key, gid, lane);
+            });
+        } else if (MODE == kMassiveCount) {
+            uint32_t cnt = 0;
+            sweep_cta(me, a, s_band, lane, warp, [&](bool v, int, int) {
+                cnt += __popc(__ballot_sync(GSR_FULL_MASK, v));
+            });
+            if (lane == 0) s_wcnt[warp] = cnt;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint32_t t = 0;
+                for (int w = 0; w < kWarps; w++) t += s_wcnt[w];
+                a.df.count[gid] = t;
             }
+        } else {
+            // Gaussians that hit no tile were not ranked
+            if (a.df.count[gid] == 0u) continue;
+            const long long base = df.offsets[df.rank[gid]];
+            sweep_cta(me, a, s_band, lane, warp, [&](bool v, int x, int y) {
+                const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
+                if (!m) return;
+                uint32_t w0 = 0;
+                if (lane == 0) w0 = atomicAdd(&s_pos, (uint32_t)__popc(m));
+                w0 = __shfl_sync(GSR_FULL_MASK, w0, 0);
+                if (v) {
+                    const long long pos = base + w0 + __popc(m & lanemask_lt());
+                    if (pos < df.cap) {
+                        df.tiles[pos] = (uint32_t)(y * a.gx + x);
+                        df.vals[pos] = gid;
+                    }
+                }
+            });
         }
     }
-    block_flush(st, out, s_fill, s_base, lane, warp);
+
+    // (2) large rectangles, one warp each
+    for (;;) {
+        int e = 0;
+        if (lane == 0) e = (int)atomicAdd(&head[1], 1u);
+        e = __shfl_sync(GSR_FULL_MASK, e, 0);
+        if (e >= n_large) break;
+        const MassiveEntry me = a.mq.entries[a.mq.huge_capacity + e];
+        const uint32_t db = __float_as_uint(me.ctr_power_depth.w);
+        const uint32_t gid = __float_as_uint(me.conic_gid.w);
+        if (MODE == kMassiveEmit64) {
+            sweep_warp(me, a, lane, [&](bool v, int x, int y) {
+                uint64_t key = ((uint64_t)(uint32_t)(y * a.gx + x) << 32) | db;
+                stage_emit(st, out, v, key, gid, lane);
+            });
+        } else if (MODE == kMassiveCount) {
+            uint32_t cnt = 0;
+            sweep_warp(me, a, lane, [&](bool v, int, int) { cnt += __popc(__ballot_sync(GSR_FULL_MASK, v)); });
+            if (lane == 0) a.df.count[gid] = cnt;
+        } else {
+            if (a.df.count[gid] == 0u) continue;
+            const long long base = df.offsets[df.rank[gid]];
+            uint32_t wpos = 0;
+            sweep_warp(me, a, lane, [&](bool v, int x, int y) {
+                const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
+                if (v) {
+                    const long long pos = base + wpos + __popc(m & lanemask_lt());
+                    if (pos < df.cap) {
+                        df.tiles[pos] = (uint32_t)(y * a.gx + x);
+                        df.vals[pos] = gid;
+                    }
+                }
+                wpos += __popc(m);
+            });
+        }
+    }
+    if (MODE == kMassiveEmit64) block_flush(st, out, s_fill, s_base, lane, warp);
+}
+
+// Depth-first emission of the Gaussians that were not queued: one thread per
+// Gaussian, taken in depth order, writes its (tile, index) pairs from its
+// offset on.  Same tile test as the counting pass, so exactly count[g] pairs.
+__global__ __launch_bounds__(256) void k_df_emit_small(const PreprocessParams a, const DfEmit df,
+                                                       const uint32_t* __restrict__ d_v,
+                                                       const uint32_t* __restrict__ sgids)
+{
+    const int V = (int)min(*d_v, (uint32_t)a.P);
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < V; s += gridDim.x * blockDim.x) {
+        const uint32_t gid = __ldg(sgids + s);
+        if (gid >= (uint32_t)a.P) continue;
+        const int2 r = __ldg(a.df.rect + gid);
+        if ((uint32_t)r.y & 0x80000000u) continue;  // queued: the massive kernel writes it
+        const int x0 = r.x & 0xFFFF, x1 = (int)((uint32_t)r.x >> 16);
+        const int y0 = r.y & 0xFFFF, y1 = (int)(((uint32_t)r.y >> 16) & 0x7FFFu);
+        const float4 g = __ldg(a.df.geo + gid);
+        const float2 ctr = __ldg(a.points_xy + gid);
+        const float3 con = {g.x, g.y, g.z};
+        long long pos = __ldg(df.offsets + s);
+        for (int y = y0; y < y1; y++)
+            for (int x = x0; x < x1; x++) {
+                if (!tile_hit(x, y, a.bx, a.by, ctr, con, g.w)) continue;
+                if (pos < df.cap) {
+                    df.tiles[pos] = (uint32_t)(y * a.gx + x);
+                    df.vals[pos] = gid;
+                }
+                pos++;
+            }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -727,20 +977,60 @@ cudaError_t launch_scene_prepare(int P, const float* log_scales, const float* qu
     return cudaGetLastError();
 }
 
-cudaError_t launch_preprocess(const PreprocessParams& p, bool half_sh, cudaStream_t stream)
+static cudaError_t preprocess_common(const PreprocessParams& p, bool half_sh, bool count, cudaStream_t stream)
 {
     if (p.P <= 0) return cudaSuccess;
     if (p.mq.capacity > 0) {
-        // count, head and depth_hi are adjacent words of the workspace header
-        cudaError_t e = cudaMemsetAsync(p.mq.count, 0, 3 * sizeof(uint32_t), stream);
+        // queue counters, heads of both passes and depth_hi: the preprocess
+        // region of the workspace header, which starts at the count words
+        cudaError_t e = cudaMemsetAsync(p.mq.count, 0, kPreprocessRegionBytes, stream);
         if (e != cudaSuccess) return e;
     }
     const int grid = div_up(p.P, kThreads);
-    if (half_sh) k_preprocess<true><<<grid, kThreads, 0, stream>>>(p);
-    else k_preprocess<false><<<grid, kThreads, 0, stream>>>(p);
+    if (count) {
+        if (half_sh) k_preprocess<true, true><<<grid, kThreads, 0, stream>>>(p);
+        else k_preprocess<false, true><<<grid, kThreads, 0, stream>>>(p);
+    } else {
+        if (half_sh) k_preprocess<true, false><<<grid, kThreads, 0, stream>>>(p);
+        else k_preprocess<false, false><<<grid, kThreads, 0, stream>>>(p);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.mq.capacity <= 0) return e;
-    k_emit_massive<<<device_sm_count() * 4, kThreads, 0, stream>>>(p);
+    const DfEmit none{nullptr, nullptr, nullptr, nullptr, 0};
+    if (count) k_emit_massive<kMassiveCount><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, none);
+    else k_emit_massive<kMassiveEmit64><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, none);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_preprocess(const PreprocessParams& p, bool half_sh, cudaStream_t stream)
+{
+    return preprocess_common(p, half_sh, false, stream);
+}
+
+cudaError_t launch_preprocess_count(const PreprocessParams& p, bool half_sh, cudaStream_t stream)
+{
+    return preprocess_common(p, half_sh, true, stream);
+}
+
+cudaError_t launch_df_emit_massive(const PreprocessParams& p, const uint32_t* offsets, const uint32_t* rank,
+                                   uint32_t* tiles, uint32_t* vals, long long cap, cudaStream_t stream)
+{
+    if (p.P <= 0 || p.mq.capacity <= 0) return cudaSuccess;
+    // takes the queue again through the second pair of heads (cleared with
+    // the rest of the preprocess region before the counting pass)
+    const DfEmit df{offsets, rank, tiles, vals, cap};
+    k_emit_massive<kMassiveEmitDf><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, df);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_df_emit_small(const PreprocessParams& p, const uint32_t* d_v, const uint32_t* sgids,
+                                 const uint32_t* offsets, uint32_t* tiles, uint32_t* vals, long long cap,
+                                 cudaStream_t stream)
+{
+    if (p.P <= 0) return cudaSuccess;
+    const DfEmit df{offsets, nullptr, tiles, vals, cap};
+    const int grid = std::min(div_up(p.P, 256), device_sm_count() * 8);
+    k_df_emit_small<<<grid, 256, 0, stream>>>(p, df, d_v, sgids);
     return cudaGetLastError();
 }
 

@@ -21,15 +21,19 @@ __device__ __forceinline__ int clamp_count(int num, const int32_t* d_num, long l
     return (int)n;
 }
 
+__device__ __forceinline__ uint32_t tile_of(uint64_t k) { return (uint32_t)(k >> 32); }
+__device__ __forceinline__ uint32_t tile_of(uint32_t k) { return k; }
+
+template <typename K>
 __global__ void k_ranges_exact(int num, const int32_t* __restrict__ d_num, long long cap, int tiles,
-                               const uint64_t* __restrict__ keys, int2* __restrict__ ranges)
+                               const K* __restrict__ keys, int2* __restrict__ ranges)
 {
     const int n = clamp_count(num, d_num, cap);
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i <= n; i += stride) {
         int a = -1, b = tiles;  // tile(i-1), tile(i); virtual -1 and T at the ends
-        if (i > 0) a = (int)min((uint64_t)tiles, __ldg(keys + i - 1) >> 32);
-        if (i < n) b = (int)min((uint64_t)tiles, __ldg(keys + i) >> 32);
+        if (i > 0) a = (int)min((uint32_t)tiles, tile_of(__ldg(keys + i - 1)));
+        if (i < n) b = (int)min((uint32_t)tiles, tile_of(__ldg(keys + i)));
         if (a == b) continue;
         // start = i for tiles a+1 .. b (capped at T-1); end = i for tiles max(a,0) .. b-1
         const int lo = max(a, 0), hi = min(b, tiles - 1);
@@ -98,8 +102,18 @@ cudaError_t launch_tile_ranges(int num, const int32_t* d_num, long long cap, int
         k_zero_ranges<<<min(sms * 4, div_up(tiles, 256)), 256, 0, stream>>>(tiles, r);
         k_ranges_scan<<<grid, 256, 0, stream>>>(num, d_num, cap, tiles, keys, r);
     } else {
-        k_ranges_exact<<<grid, 256, 0, stream>>>(num, d_num, cap, tiles, keys, r);
+        k_ranges_exact<uint64_t><<<grid, 256, 0, stream>>>(num, d_num, cap, tiles, keys, r);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tile_ranges32(const int32_t* d_num, long long cap, int tiles, const uint32_t* tile_ids,
+                                 int2* ranges, cudaStream_t stream)
+{
+    if (tiles <= 0) return cudaSuccess;
+    const int sms = device_sm_count();
+    const int grid = (int)max(1LL, min((long long)sms * 8, (cap + 256) / 256));
+    k_ranges_exact<uint32_t><<<grid, 256, 0, stream>>>(0, d_num, cap, tiles, tile_ids, ranges);
     return cudaGetLastError();
 }
 

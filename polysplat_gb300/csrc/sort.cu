@@ -1,10 +1,11 @@
-// Stable LSD radix sort of (u64 key, u32 value) pairs for sm_103a.
+// Stable LSD radix sort of (key, u32 value) pairs for sm_103a, for 64-bit
+// tile|depth keys and for 32-bit keys.
 //
-// Contract (same as the reference's CUB call, csrc/cuda_rasterizer/sort.cu:
-// 107-125): ascending, stable, unsigned, over bits [0, end_bit); bits at or
-// above end_bit ride along but do not take part in the order; the inputs are
-// preserved.  The count may live on the device, so no host synchronisation
-// is needed between the producer of the keys and the sort.
+// Contract of the 64-bit sort (the reference's CUB call,
+// csrc/cuda_rasterizer/sort.cu:107-125): ascending, stable, unsigned, over
+// bits [0, end_bit); bits at or above end_bit ride along but do not take part
+// in the order; the inputs are preserved.  The count may live on the device,
+// so no host synchronisation is needed between the producer and the sort.
 //
 // Structure (one-sweep radix sort with decoupled look-back):
 //   1. k_upsweep: one read of all keys builds the 256-bin histogram of every
@@ -16,12 +17,12 @@
 //      spin, four predecessors per round trip), reorder the tile in shared
 //      memory by digit and write it out with coalesced stores.
 //
-// Depth compression (fused forward): every emitted key has a low word above
-// the bits of 0.2f and at most the header's depth_hi, so ordering by
-// (tile << nb) | (low - floor) with nb = bits(depth_hi - floor) is the same
-// order in fewer bits.  The number of passes that do work is then decided on
-// the device; the remaining launches return at once, and each pass picks its
-// source and destination buffer so that the last working pass lands in the
+// Keys are mapped to an "ordering word" before digits are taken (OrderMap):
+// the masked key, or -- for keys the preprocess emitted -- the depth bits
+// minus the bits of 0.2f, whose width the preprocess recorded in the
+// workspace header.  When fewer bits matter than the host planned for, the
+// remaining pass launches return at once, and every pass picks its source and
+// destination buffer on the device so that the last working pass lands in the
 // output.
 #include <algorithm>
 #include <cstdlib>
@@ -38,7 +39,21 @@ constexpr uint32_t kValueMask = (1u << 30) - 1u;
 constexpr int kWarpsPerCta = kSortThreads / 32;
 constexpr int kWarpItems = kSortItems * 32;  // consecutive keys per warp
 
-__device__ __forceinline__ int sort_count(const SortArgs& a)
+template <typename K>
+struct SortJob {
+    int num;
+    const int32_t* d_num;
+    long long cap;
+    OrderMap order;
+    const K* keys_in;
+    const uint32_t* vals_in;
+    K* keys_out;
+    uint32_t* vals_out;
+    SortScratch s;
+};
+
+template <typename K>
+__device__ __forceinline__ int sort_count(const SortJob<K>& a)
 {
     long long n = a.d_num ? (long long)*a.d_num : (long long)a.num;
     if (n < 0) n = 0;
@@ -46,107 +61,96 @@ __device__ __forceinline__ int sort_count(const SortArgs& a)
     return (int)n;
 }
 
-struct Layout {
-    WorkspaceHeader* hdr;
-    uint64_t* alt_keys;
-    uint32_t* alt_vals;
-    uint32_t* look[2];
-    long long tiles_cap;
-};
-
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-__host__ __device__ inline Layout make_layout(void* ws, long long cap)
-{
-    Layout L;
-    char* p = reinterpret_cast<char*>(ws);
-    L.hdr = reinterpret_cast<WorkspaceHeader*>(p);
-    size_t off = kSmallWorkspaceBytes;  // header + massive-Gaussian queue
-    L.alt_keys = reinterpret_cast<uint64_t*>(p + off);
-    off += align256((size_t)cap * 8);
-    L.alt_vals = reinterpret_cast<uint32_t*>(p + off);
-    off += align256((size_t)cap * 4);
-    L.tiles_cap = (cap + kSortTile - 1) / kSortTile;
-    L.look[0] = reinterpret_cast<uint32_t*>(p + off);
-    off += align256((size_t)L.tiles_cap * 256 * 4);
-    L.look[1] = reinterpret_cast<uint32_t*>(p + off);
-    return L;
-}
-
-// The ordering word of a key and the number of its bits that matter.
+// The ordering word of a key and how many of its bits matter.
 struct KeyMap {
-    int bits;           // significant bits of the ordering word
-    int depth_bits;     // 0: no compression
-    uint64_t mask;      // mask of the uncompressed key (end_bit bits)
+    int kind;
+    int bits;
+    int depth_bits;
+    uint64_t mask;
     uint32_t tile_mask;
 };
 
-__device__ __forceinline__ KeyMap key_map(const SortArgs& a, const Layout& L)
+__device__ __forceinline__ int depth_width(const WorkspaceHeader* h)
+{
+    const uint32_t hi = h->depth_hi;
+    return hi > kDepthBitsFloor ? bits_for(hi - kDepthBitsFloor) : 0;
+}
+
+__device__ __forceinline__ KeyMap key_map(const OrderMap& o, const WorkspaceHeader* h)
 {
     KeyMap m;
-    m.mask = a.end_bit >= 64 ? ~0ull : ((1ull << a.end_bit) - 1ull);
+    m.kind = o.kind;
     m.depth_bits = 0;
     m.tile_mask = 0;
-    m.bits = a.end_bit;
-    if (a.compress_depth && a.end_bit > 32) {
-        const uint32_t hi = L.hdr->depth_hi;
-        const int nb = hi > kDepthBitsFloor ? bits_for(hi - kDepthBitsFloor) : 0;
-        m.depth_bits = nb;
-        m.tile_mask = (uint32_t)((1ull << (a.end_bit - 32)) - 1ull);
-        m.bits = (a.end_bit - 32) + nb;
-        if (m.bits < 1) m.bits = 1;
+    m.bits = o.end_bit;
+    m.mask = o.end_bit >= 64 ? ~0ull : ((1ull << o.end_bit) - 1ull);
+    if (o.kind == kOrderDepthCompressed64) {
+        m.depth_bits = depth_width(h);
+        m.tile_mask = (uint32_t)((1ull << (o.end_bit - 32)) - 1ull);
+        m.bits = (o.end_bit - 32) + m.depth_bits;
+    } else if (o.kind == kOrderDepth32) {
+        m.bits = depth_width(h);
     }
+    if (m.bits < 1) m.bits = 1;
     return m;
 }
 
 __device__ __forceinline__ uint64_t order_word(uint64_t k, const KeyMap& m)
 {
-    if (m.tile_mask == 0) return k & m.mask;
-    const uint64_t tile = (uint64_t)((uint32_t)(k >> 32) & m.tile_mask);
-    return (tile << m.depth_bits) | (uint64_t)((uint32_t)k - kDepthBitsFloor);
+    if (m.kind == kOrderDepthCompressed64) {
+        const uint64_t tile = (uint64_t)((uint32_t)(k >> 32) & m.tile_mask);
+        return (tile << m.depth_bits) | (uint64_t)((uint32_t)k - kDepthBitsFloor);
+    }
+    return k & m.mask;
+}
+
+__device__ __forceinline__ uint64_t order_word(uint32_t k, const KeyMap& m)
+{
+    if (m.kind == kOrderDepth32) return (uint64_t)(k - kDepthBitsFloor);
+    return (uint64_t)k & m.mask;
 }
 
 __device__ __forceinline__ int passes_of(const KeyMap& m) { return (m.bits + 7) / 8; }
+
+template <typename K>
+__device__ __forceinline__ void load8(const K* src, long long b, int cnt, K (&k)[8])
+{
+#pragma unroll
+    for (int j = 0; j < 8; j++) k[j] = j < cnt ? __ldg(src + b + j) : K(0);
+}
 
 // ---------------------------------------------------------------------------
 // Histogram of every digit pass.  Each thread takes runs of 8 consecutive keys
 // and merges equal consecutive digits before touching shared memory: keys of
 // one Gaussian are emitted together and share their depth digits, so this
 // removes most same-address shared atomics.
-__global__ __launch_bounds__(256) void k_upsweep(SortArgs a, Layout L, int max_passes)
+template <typename K>
+__global__ __launch_bounds__(256) void k_upsweep(SortJob<K> a, int max_passes)
 {
     __shared__ uint32_t s_hist[kMaxPasses][256];
     for (int i = threadIdx.x; i < kMaxPasses * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0u;
     __syncthreads();
     const int n = sort_count(a);
     const int tiles = (n + kSortTile - 1) / kSortTile;
-    const KeyMap km = key_map(a, L);
+    const KeyMap km = key_map(a.order, a.s.hdr);
     const int passes = min(max_passes, passes_of(km));
     // clear the look-back state used by the first digit pass
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)tiles * 256;
          i += (long long)gridDim.x * blockDim.x)
-        L.look[0][i] = 0u;
+        a.s.look[0][i] = 0u;
 
     const long long runs = (n + 7) / 8;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < runs;
          r += (long long)gridDim.x * blockDim.x) {
         const long long b = r * 8;
-        uint64_t k[8];
+        K kk[8];
         const int cnt = (int)min(8LL, (long long)n - b);
-        if (cnt == 8 && ((reinterpret_cast<uintptr_t>(a.keys_in + b) & 15) == 0)) {
-            const uint4* src = reinterpret_cast<const uint4*>(a.keys_in + b);
+        load8(a.keys_in, b, cnt, kk);
+        uint64_t k[8];
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                uint4 v = __ldg(src + j);
-                k[2 * j] = ((uint64_t)v.y << 32) | v.x;
-                k[2 * j + 1] = ((uint64_t)v.w << 32) | v.z;
-            }
-        } else {
-#pragma unroll
-            for (int j = 0; j < 8; j++) k[j] = j < cnt ? __ldg(a.keys_in + b + j) : 0ull;
-        }
-#pragma unroll
-        for (int j = 0; j < 8; j++) k[j] = order_word(k[j], km);
+        for (int j = 0; j < 8; j++) k[j] = order_word(kk[j], km);
         for (int p = 0; p < passes; p++) {
             const int shift = 8 * p;
             uint32_t cur = (uint32_t)(k[0] >> shift) & 0xFFu;
@@ -169,13 +173,14 @@ __global__ __launch_bounds__(256) void k_upsweep(SortArgs a, Layout L, int max_p
     __syncthreads();
     for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
         uint32_t v = (&s_hist[0][0])[i];
-        if (v) atomicAdd(&L.hdr->hist[0][0] + i, v);
+        if (v) atomicAdd(&a.s.hdr->hist[0][0] + i, v);
     }
 }
 
 // ---------------------------------------------------------------------------
+template <typename K>
 struct PassSmem {
-    uint64_t keys[kSortTile];
+    K keys[kSortTile];
     uint32_t vals[kSortTile];
     uint32_t whist[kWarpsPerCta][256];  // per-warp digit counts, then warp-exclusive offsets
     uint32_t digit_excl[256];           // tile-local start of each digit
@@ -205,24 +210,15 @@ __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* war
     return wpre + incl - v;
 }
 
-struct PassBuffers {
-    const uint64_t* keys_in;
-    const uint32_t* vals_in;
-    uint64_t* keys_out;
-    uint32_t* vals_out;
-    uint64_t* keys_alt;
-    uint32_t* vals_alt;
-};
-
-// MATCH: per-warp ranking with match.any (one instruction per key);
-// otherwise with one ballot per digit bit.
-template <bool MATCH>
-__global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortArgs a, Layout L, int pass, PassBuffers B)
+// One digit pass.  MATCH: per-warp ranking with match.any (one instruction
+// per key), otherwise one ballot per digit bit.
+template <typename K, bool MATCH>
+__global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortJob<K> a, int pass)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    PassSmem& S = *reinterpret_cast<PassSmem*>(smem_raw);
+    PassSmem<K>& S = *reinterpret_cast<PassSmem<K>*>(smem_raw);
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const KeyMap km = key_map(a, L);
+    const KeyMap km = key_map(a.order, a.s.hdr);
     const int passes = passes_of(km);
     if (pass >= passes) return;  // nothing left to order in this digit
     const int n = sort_count(a);
@@ -231,23 +227,26 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortArgs a, Layout L, 
     const int bits = min(8, km.bits - shift);
     // ping-pong so that the last working pass writes the output buffers
     const bool to_out = ((passes - 1 - pass) & 1) == 0;
-    const uint64_t* kin = B.keys_in;
-    const uint32_t* vin = B.vals_in;
+    K* alt_k = reinterpret_cast<K*>(a.s.alt_keys);
+    const K* kin = a.keys_in;
+    const uint32_t* vin = a.vals_in;
     if (pass > 0) {
         const bool prev_out = ((passes - pass) & 1) == 0;
-        kin = prev_out ? B.keys_out : B.keys_alt;
-        vin = prev_out ? B.vals_out : B.vals_alt;
+        kin = prev_out ? a.keys_out : alt_k;
+        vin = prev_out ? a.vals_out : a.s.alt_vals;
     }
-    uint64_t* kout = to_out ? B.keys_out : B.keys_alt;
-    uint32_t* vout = to_out ? B.vals_out : B.vals_alt;
-    uint32_t* look = L.look[pass & 1];
-    uint32_t* look_next = L.look[(pass + 1) & 1];
+    K* kout = to_out ? a.keys_out : alt_k;
+    uint32_t* vout = to_out ? a.vals_out : a.s.alt_vals;
+    // selects rather than a dynamic index, so the parameter block stays out of local memory
+    uint32_t* look = (pass & 1) ? a.s.look[1] : a.s.look[0];
+    uint32_t* look_next = (pass & 1) ? a.s.look[0] : a.s.look[1];
     const bool clear_next = pass + 1 < passes;
+    WorkspaceHeader* hdr = a.s.hdr;
 
-    S.gstart[threadIdx.x] = block_excl_scan256(L.hdr->hist[pass][threadIdx.x], S.warp_sums);
+    S.gstart[threadIdx.x] = block_excl_scan256(hdr->hist[pass][threadIdx.x], S.warp_sums);
 
     for (;;) {
-        if (threadIdx.x == 0) S.tile = (int)atomicAdd(&L.hdr->pass_counter[pass], 1u);
+        if (threadIdx.x == 0) S.tile = (int)atomicAdd(&hdr->pass_counter[pass], 1u);
         for (int i = threadIdx.x; i < kWarpsPerCta * 256; i += kSortThreads) (&S.whist[0][0])[i] = 0u;
         __syncthreads();
         const int tile = S.tile;
@@ -257,7 +256,7 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortArgs a, Layout L, 
         if (clear_next) look_next[(size_t)tile * 256 + threadIdx.x] = 0u;
 
         // ---- load (warp-contiguous chunk) + stable per-warp rank ----
-        uint64_t key[kSortItems];
+        K key[kSortItems];
         uint32_t val[kSortItems];
         uint32_t dig[kSortItems];
         uint32_t rank[kSortItems];
@@ -269,7 +268,7 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortArgs a, Layout L, 
                 key[i] = kin[tbase + o];
                 val[i] = vin[tbase + o];
             } else {
-                key[i] = 0ull;
+                key[i] = K(0);
                 val[i] = 0u;
             }
         }
@@ -348,7 +347,7 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortArgs a, Layout L, 
                 }
                 if (!done && (v[0] & ~kValueMask) == 0u) {
                     if (++spins > kSpinLimit) {
-                        record_error(&L.hdr->status, kErrTimeout);
+                        record_error(&hdr->status, kErrTimeout);
                         break;
                     }
                     __nanosleep(32);
@@ -372,7 +371,7 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortArgs a, Layout L, 
         __syncthreads();
         bool oob = false;
         for (int p = threadIdx.x; p < tcount; p += kSortThreads) {
-            const uint64_t k = S.keys[p];
+            const K k = S.keys[p];
             const uint32_t d = (uint32_t)(order_word(k, km) >> shift) & ((1u << bits) - 1u);
             const long long g = (long long)S.gofs[d] + p;
             if (g < 0 || g >= n) {  // only after a look-back timeout: never write outside the buffer
@@ -382,7 +381,7 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortArgs a, Layout L, 
             kout[g] = k;
             vout[g] = S.vals[p];
         }
-        if (oob) record_error(&L.hdr->status, kErrTimeout);
+        if (oob) record_error(&hdr->status, kErrTimeout);
         __syncthreads();
     }
 }
@@ -397,7 +396,47 @@ bool use_match_ranking()
     return mode == 1;
 }
 
+template <typename K>
+cudaError_t run_sort(const SortJob<K>& a, int max_passes, cudaStream_t stream)
+{
+    if (a.cap >= (1LL << 30) || max_passes < 1 || max_passes > kMaxPasses) return cudaErrorInvalidValue;
+    // clear the sort region of the header (pass counters and histograms)
+    cudaError_t e = cudaMemsetAsync(reinterpret_cast<char*>(a.s.hdr) + kSortRegionOffset, 0,
+                                    sizeof(WorkspaceHeader) - kSortRegionOffset, stream);
+    if (e != cudaSuccess) return e;
+    const int sms = device_sm_count();
+    int up_grid = (int)std::min<long long>((long long)sms * 4, std::max<long long>(1, (a.cap + 2047) / 2048));
+    k_upsweep<K><<<up_grid, 256, 0, stream>>>(a, max_passes);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    profile_mark(stream);
+
+    const bool match = use_match_ranking();
+    auto kern = match ? k_pass<K, true> : k_pass<K, false>;
+    static bool attr_set[2] = {false, false};
+    const int smem = (int)sizeof(PassSmem<K>);
+    if (!attr_set[match]) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr_set[match] = true;
+    }
+    static int per_sm[2] = {0, 0};
+    if (per_sm[match] == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kSortThreads, smem) != cudaSuccess || b < 1) b = 1;
+        per_sm[match] = b;
+    }
+    const int grid = (int)std::min<long long>((long long)sms * per_sm[match], std::max<long long>(1, a.s.tiles_cap));
+    for (int p = 0; p < max_passes; p++) {
+        kern<<<grid, kSortThreads, smem, stream>>>(a, p);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        profile_mark(stream);
+    }
+    return cudaSuccess;
+}
+
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Workspace layout: [header+queue][alt keys 8*cap][alt vals 4*cap][look-back x2][tile ranges]
 
 static size_t sort_area_bytes(long long cap)
 {
@@ -414,46 +453,80 @@ int2* workspace_ranges(void* ws, long long cap)
     return reinterpret_cast<int2*>(reinterpret_cast<char*>(ws) + sort_area_bytes(cap));
 }
 
+SortScratch workspace_sort_scratch(void* ws, long long cap)
+{
+    SortScratch s;
+    char* p = reinterpret_cast<char*>(ws);
+    s.hdr = reinterpret_cast<WorkspaceHeader*>(p);
+    size_t off = kSmallWorkspaceBytes;
+    s.alt_keys = p + off;
+    off += align256((size_t)(cap < 1 ? 1 : cap) * 8);
+    s.alt_vals = reinterpret_cast<uint32_t*>(p + off);
+    off += align256((size_t)(cap < 1 ? 1 : cap) * 4);
+    s.tiles_cap = ((cap < 1 ? 1 : cap) + kSortTile - 1) / kSortTile;
+    s.look[0] = reinterpret_cast<uint32_t*>(p + off);
+    off += align256((size_t)s.tiles_cap * 256 * 4);
+    s.look[1] = reinterpret_cast<uint32_t*>(p + off);
+    return s;
+}
+
+size_t sort_scratch_bytes(long long cap, int key_bytes)
+{
+    if (cap < 1) cap = 1;
+    long long tiles = (cap + kSortTile - 1) / kSortTile;
+    return align256((size_t)cap * key_bytes) + align256((size_t)cap * 4) + 2 * align256((size_t)tiles * 256 * 4);
+}
+
+SortScratch carve_sort_scratch(WorkspaceHeader* hdr, void* mem, long long cap, int key_bytes)
+{
+    SortScratch s;
+    char* p = reinterpret_cast<char*>(mem);
+    s.hdr = hdr;
+    if (cap < 1) cap = 1;
+    s.alt_keys = p;
+    size_t off = align256((size_t)cap * key_bytes);
+    s.alt_vals = reinterpret_cast<uint32_t*>(p + off);
+    off += align256((size_t)cap * 4);
+    s.tiles_cap = (cap + kSortTile - 1) / kSortTile;
+    s.look[0] = reinterpret_cast<uint32_t*>(p + off);
+    off += align256((size_t)s.tiles_cap * 256 * 4);
+    s.look[1] = reinterpret_cast<uint32_t*>(p + off);
+    return s;
+}
+
 cudaError_t launch_sort(const SortArgs& a, cudaStream_t stream)
 {
     if (a.end_bit < 1 || a.end_bit > 64) return cudaErrorInvalidValue;
     if (a.ws_bytes < sort_area_bytes(a.cap)) return cudaErrorInvalidValue;
-    if (a.cap >= (1LL << 30)) return cudaErrorInvalidValue;
-    Layout L = make_layout(a.ws, a.cap);
-    const int passes = (a.end_bit + 7) / 8;  // upper bound; the device may need fewer
-    // clear the sort region of the header (pass counters and histograms)
-    cudaError_t e = cudaMemsetAsync(reinterpret_cast<char*>(L.hdr) + kSortRegionOffset, 0,
-                                    sizeof(WorkspaceHeader) - kSortRegionOffset, stream);
-    if (e != cudaSuccess) return e;
-    const int sms = device_sm_count();
-    const long long tiles_cap = L.tiles_cap;
-    int up_grid = (int)std::min<long long>((long long)sms * 4, std::max<long long>(1, (a.cap + 2047) / 2048));
-    k_upsweep<<<up_grid, 256, 0, stream>>>(a, L, passes);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    profile_mark(stream);
+    SortJob<uint64_t> j;
+    j.num = a.num;
+    j.d_num = a.d_num;
+    j.cap = a.cap;
+    j.order.kind = a.compress_depth && a.end_bit > 32 ? kOrderDepthCompressed64 : kOrderMasked;
+    j.order.end_bit = a.end_bit;
+    j.keys_in = a.keys_in;
+    j.vals_in = a.vals_in;
+    j.keys_out = a.keys_out;
+    j.vals_out = a.vals_out;
+    j.s = workspace_sort_scratch(a.ws, a.cap);
+    return run_sort(j, (a.end_bit + 7) / 8, stream);
+}
 
-    const bool match = use_match_ranking();
-    auto kern = match ? k_pass<true> : k_pass<false>;
-    static bool attr_set[2] = {false, false};
-    const int smem = (int)sizeof(PassSmem);
-    if (!attr_set[match]) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        attr_set[match] = true;
-    }
-    static int per_sm[2] = {0, 0};
-    if (per_sm[match] == 0) {
-        int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kSortThreads, smem) != cudaSuccess || b < 1) b = 1;
-        per_sm[match] = b;
-    }
-    const int grid = (int)std::min<long long>((long long)sms * per_sm[match], std::max<long long>(1, tiles_cap));
-    PassBuffers B{a.keys_in, a.vals_in, a.keys_out, a.vals_out, L.alt_keys, L.alt_vals};
-    for (int p = 0; p < passes; p++) {
-        kern<<<grid, kSortThreads, smem, stream>>>(a, L, p, B);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        profile_mark(stream);
-    }
-    return cudaSuccess;
+cudaError_t launch_sort32(int num, const int32_t* d_num, long long cap, OrderMap order, int max_passes,
+                          const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                          const SortScratch& s, cudaStream_t stream)
+{
+    SortJob<uint32_t> j;
+    j.num = num;
+    j.d_num = d_num;
+    j.cap = cap;
+    j.order = order;
+    j.keys_in = keys_in;
+    j.vals_in = vals_in;
+    j.keys_out = keys_out;
+    j.vals_out = vals_out;
+    j.s = s;
+    return run_sort(j, max_passes, stream);
 }
 
 }  // namespace gsr

@@ -574,6 +574,47 @@ def _forward(variant, half, orig_points, shs, opacities, cov3Ds, width, height, 
     return _read_status(ws, curr_offset, cap, "forward")
 
 
+def depth_first_scratch_size(P):
+    """Bytes of per-Gaussian scratch the depth-first forward needs (library extension)."""
+    return int(lib().gsr_depth_first_scratch_size(int(P)))
+
+
+def forward_depth_first(variant, half, orig_points, shs, opacities, cov3Ds, width, height, block_x, block_y, position,
+                        rotation, focal_x, focal_y, zFar, zNear, curr_offset, list_sorting_space, scene_scratch,
+                        tiles_unsorted, values_unsorted, tiles_sorted, values_sorted, points_xy, rgb_depth,
+                        conic_opacity, ranges, bg_color, out_color):
+    """Depth-first ("early sorting") forward in one call (library extension;
+    the reference's two-pass ES pipeline, csrc/cuda_rasterizer/preprocess.cu:673-1248,
+    sort.cu:151-285).  Tile ids and values are int32 tensors of the key
+    capacity; returns the pair count M."""
+    pos = _dev(orig_points, "orig_points", torch.float32)
+    sh = _dev(shs, "shs", torch.float16 if half else torch.float32)
+    op = _dev(opacities, "opacities", torch.float32)
+    cov = _dev(cov3Ds, "cov3Ds", torch.float32)
+    ws = _dev(list_sorting_space, "list_sorting_space")
+    sc = _dev(scene_scratch, "scene_scratch")
+    for t, nm, dt in ((curr_offset, "curr_offset", torch.int32), (tiles_unsorted, "tiles_unsorted", torch.int32),
+                      (values_unsorted, "values_unsorted", torch.int32), (tiles_sorted, "tiles_sorted", torch.int32),
+                      (values_sorted, "values_sorted", torch.int32), (points_xy, "points_xy", torch.float32),
+                      (rgb_depth, "rgb_depth", torch.float32), (conic_opacity, "conic_opacity", torch.float32),
+                      (out_color, "out_color", torch.uint8)):
+        _dev(t, nm, dt)
+    if ranges is not None:
+        _dev(ranges, "tile_ranges_buf", torch.int32)
+    wsb = ws.numel() * ws.element_size()
+    cap = _sort_capacity(0, wsb, tiles_unsorted, values_unsorted, tiles_sorted, values_sorted)
+    st = lib().gsr_forward_depth_first(
+        int(variant), op.numel(), _ptr(pos), _ptr(sh), 1 if half else 0, _ptr(op), _ptr(cov), int(width),
+        int(height), int(block_x), int(block_y), _host_floats(position, 3, "position"),
+        _host_floats(rotation, 9, "rotation"), float(focal_x), float(focal_y), float(zFar), float(zNear),
+        _ptr(curr_offset), _ptr(ws), wsb, _ptr(sc), sc.numel() * sc.element_size(), _ptr(tiles_unsorted),
+        _ptr(values_unsorted), _ptr(tiles_sorted), _ptr(values_sorted), cap, _ptr(points_xy), _ptr(rgb_depth),
+        _ptr(conic_opacity), _ptr(ranges) if ranges is not None else None, _host_floats(bg_color, 3, "bg_color"),
+        _ptr(out_color), _stream(ws.device))
+    check(st, "forward_depth_first")
+    return _read_status(ws, curr_offset, cap, "forward_depth_first")
+
+
 def _variant_code(render_variant: str, block_x: int, block_y: int) -> int:
     if render_variant in ("default", "unroll2", "split"):
         return R.RENDER_DEFAULT
