@@ -119,6 +119,19 @@ gsr_status gsr_sort_bits(int num, const int32_t* d_num, int end_bit, void* works
                          const uint64_t* keys_in, const uint32_t* values_in, uint64_t* keys_out,
                          uint32_t* values_out, int64_t capacity, gsr_stream_t stream);
 
+/* Same sort as gsr_sort_bits, with no workspace argument and no allocation:
+ * no counterpart in the reference.  For callers that cannot allocate or
+ * hold device scratch (a thin FFI host that owns only the key/value buffers;
+ * latency-bound loops that must not call cudaMalloc, which can synchronise
+ * the device).  Scratch is a library-owned static device array sized for
+ * capacity <= 262144 pairs; larger capacities return GSR_INVALID_ARG.  The
+ * first call on each device looks up that array's address (make it before
+ * any stream capture on that device).  All calls share the array: calls that
+ * overlap in time race and must be serialised by the caller. */
+gsr_status gsr_sort_bits_static(int num, const int32_t* d_num, int end_bit, const uint64_t* keys_in,
+                                const uint32_t* values_in, uint64_t* keys_out, uint32_t* values_out,
+                                int64_t capacity, gsr_stream_t stream);
+
 /* ---- tile ranges / gather ----------------------------------------------- */
 /* ranges[t] = [first, end) of tile t in the sorted keys.  scan_semantics = 0
  * reproduces precompute_tile_ranges (binary search: empty tiles get

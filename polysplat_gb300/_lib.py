@@ -57,6 +57,7 @@ def _declare(L):
         "gsr_forward": ([i32, i32, P, P, i32, P, P, i32, i32, i32, i32, P, P, f32, f32, f32, f32,
                          P, P, sz, P, P, P, P, i64, P, P, P, P, P, P, P], i32),
     }
+    sig["gsr_sort_bits_static"] = ([i32, P, i32, P, P, P, P, i64, P], i32)
     sig["gsr_depth_first_scratch_size"] = ([i32], sz)
     sig["gsr_forward_depth_first"] = ([i32, i32, P, P, i32, P, P, i32, i32, i32, i32, P, P, f32, f32, f32, f32,
                                        P, P, sz, P, sz, P, P, P, P, i64, P, P, P, P, P, P, P], i32)

@@ -168,6 +168,9 @@ SortScratch workspace_sort_scratch(void* ws, long long cap);
 cudaError_t launch_sort32(int num, const int32_t* d_num, long long cap, OrderMap order, int max_passes,
                           const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                           const SortScratch& s, cudaStream_t stream);
+cudaError_t launch_sort64(int num, const int32_t* d_num, long long cap, OrderMap order, int max_passes,
+                          const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out, uint32_t* vals_out,
+                          const SortScratch& s, cudaStream_t stream);
 
 cudaError_t launch_tile_ranges(int num, const int32_t* d_num, long long cap, int tiles, const uint64_t* keys,
                                int32_t* ranges, bool scan_semantics, cudaStream_t stream);

@@ -529,4 +529,21 @@ cudaError_t launch_sort32(int num, const int32_t* d_num, long long cap, OrderMap
     return run_sort(j, max_passes, stream);
 }
 
+cudaError_t launch_sort64(int num, const int32_t* d_num, long long cap, OrderMap order, int max_passes,
+                          const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out, uint32_t* vals_out,
+                          const SortScratch& s, cudaStream_t stream)
+{
+    SortJob<uint64_t> j;
+    j.num = num;
+    j.d_num = d_num;
+    j.cap = cap;
+    j.order = order;
+    j.keys_in = keys_in;
+    j.vals_in = vals_in;
+    j.keys_out = keys_out;
+    j.vals_out = vals_out;
+    j.s = s;
+    return run_sort(j, max_passes, stream);
+}
+
 }  // namespace gsr
