@@ -42,7 +42,7 @@ E2E_VARIANT = "preranges_smem_persistent_lite_e2e"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", default="plain_3m_1080p")
     ap.add_argument("--impl", default="gsr", choices=["gsr", "reference", "reference-gpu"])

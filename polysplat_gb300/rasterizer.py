@@ -113,6 +113,15 @@ class Rasterizer:
         self.conic_opacity = torch.zeros((P, 4), device=dev, dtype=torch.float32)
         self.tile_ranges_buf = torch.zeros((self.MAX_NUM_TILES, 2), device=dev, dtype=torch.int32)
         self.enable_es = enable_es
+        # adaptive choice of the depth-first ("early sorting") pipeline, with
+        # the reference's thresholds and environment overrides (example.py:70-90)
+        self._es_threshold_M = int(os.environ.get("POLYSPLAT_ES_THRESHOLD_M", "5000000"))
+        self._es_threshold_N_firstcall = int(os.environ.get("POLYSPLAT_ES_THRESHOLD_N", "3000000"))
+        self._es_ratio_thresh = float(os.environ.get("POLYSPLAT_ES_RATIO_THRESH", "0.7"))
+        self._es_firstcall_huge_P_guard = int(os.environ.get("POLYSPLAT_ES_FIRSTCALL_HUGE_P", "30000000"))
+        self._es_force_two_pass = os.environ.get("POLYSPLAT_ES_FORCE_TWO_PASS", "0") not in ("0", "", "false",
+                                                                                          "False")
+        self._df_scratch = None
         self._compact = None
         self._out_color = None
         self._auto_render_choice = None
@@ -154,6 +163,53 @@ class Rasterizer:
         self._auto_render_choice = best
         return best
 
+    # -- depth-first ("early sorting") routing (example.py:246-291) ------------------
+    def _decide_use_es(self, scene, use_es, render_variant):
+        """The reference's rule: never for the fused E2E variants; True/False
+        as given; "auto" takes it when the last frame's key count M is large
+        in absolute terms and relative to P, or on a first call when P is
+        large but below the huge-scene guard."""
+        if not self.enable_es or render_variant in (E2E, E2E_PRERANGES):
+            return False
+        if use_es is True or use_es is False:
+            return use_es
+        if self._es_force_two_pass:
+            return True
+        P = scene.num_vertex
+        if self._es_last_M is not None:
+            M = self._es_last_M
+            return M > self._es_threshold_M and M > self._es_ratio_thresh * P
+        if P > self._es_firstcall_huge_P_guard:
+            return False
+        return P > self._es_threshold_N_firstcall
+
+    @staticmethod
+    def _df_variant(render_variant):
+        from . import _lib as R
+        if render_variant.endswith("_dt"):
+            return R.RENDER_DT
+        if render_variant == LITE or render_variant.startswith("preranges_smem_persistent"):
+            return R.RENDER_PERSISTENT_RANGES
+        if render_variant.startswith("preranges") or render_variant.startswith("reordered"):
+            return R.RENDER_RANGES_CADENCE2
+        return R.RENDER_DEFAULT
+
+    def _forward_depth_first(self, scene, args_cam, render_variant, bg_color, out):
+        n = self.MAX_NUM_RENDERED
+        if self._df_scratch is None:
+            self._df_scratch = torch.zeros(ops.depth_first_scratch_size(scene.num_vertex), device=self.device,
+                                           dtype=torch.int8)
+        half = render_variant.startswith("preranges_smem")
+        # 32-bit tile ids live in the front half of the 64-bit key buffers
+        tiles_u = self.gaussian_keys_unsorted.view(torch.int32)[:n]
+        tiles_s = self.gaussian_keys_sorted.view(torch.int32)[:n]
+        return ops.forward_depth_first(self._df_variant(render_variant), half, scene.position,
+                                       scene.shs_half if half else scene.shs, scene.opacity, scene.cov3d,
+                                       *args_cam, self.curr_offset, self.list_sorting_space, self._df_scratch,
+                                       tiles_u, self.gaussian_values_unsorted, tiles_s, self.gaussian_values_sorted,
+                                       self.points_xy, self.rgb_depth, self.conic_opacity, self.tile_ranges_buf,
+                                       bg_color, out)
+
     # -- forward --------------------------------------------------------------------
     def forward(self, scene, camera, bg_color, block_x=16, block_y=16, render_variant="default",
                 measure_preprocess=False, measure_sort=False, measure_render=False, return_stats=False,
@@ -175,7 +231,11 @@ class Rasterizer:
         feats = (self.points_xy, self.rgb_depth, self.conic_opacity)
 
         fused = None
-        if not measuring:
+        used_es = False
+        if not measuring and self._decide_use_es(scene, use_es, render_variant):
+            used_es = True
+            fused = lambda: self._forward_depth_first(scene, args_cam, render_variant, bg_color, out)
+        elif not measuring:
             if render_variant == E2E:
                 fused = lambda: ops.forward_fused_e2e(scene.position, scene.shs_half, scene.opacity, scene.cov3d,
                                                       *args_cam, self.curr_offset, self.list_sorting_space, *bufs,
@@ -192,7 +252,8 @@ class Rasterizer:
             num = fused()
             self._es_last_M = num
             if return_stats:
-                return out, self._stats(requested, render_variant, block_x, block_y, num, None, None, None, False)
+                return out, self._stats(requested, render_variant, block_x, block_y, num, None, None, None,
+                                        used_es)
             return out
 
         # ---- per-stage path (example.py:481-781) ----

@@ -141,3 +141,23 @@ def test_depth_first_empty_view(cuda_device):
     assert m == 0
     exp = np.clip(bg.numpy().astype(np.float32) * np.float32(255.0), 0, 255).astype(np.uint8)  # truncating encode
     assert (f.out.cpu().numpy() == exp).all()
+
+
+@pytest.mark.parametrize("variant", ["default", "preranges_smem_persistent_lite", "preranges_smem_persistent_lite_e2e"])
+def test_rasterizer_use_es_routes_to_depth_first(cuda_device, variant):
+    from polysplat_gb300 import Rasterizer
+
+    raw, cam = CASES["clustered_640x360"][0](), CASES["clustered_640x360"][1]()
+    scene = Scene.from_raw(raw, cuda_device)
+    c = Camera.from_spec(cam)
+    rast = Rasterizer(scene, 4_000_000, 1 << 16)
+    bg = torch.zeros(3)
+    a, sa = rast.forward(scene, c, bg, render_variant=variant, use_es=False, return_stats=True)
+    a = a.clone()
+    b, sb = rast.forward(scene, c, bg, render_variant=variant, use_es=True, return_stats=True)
+    torch.cuda.synchronize()
+    # the fused E2E variants never take the depth-first path (example.py:260-266)
+    assert sb["used_es"] == (not variant.endswith("_e2e")) and not sa["used_es"]
+    assert sa["num_rendered"] == sb["num_rendered"]
+    s = image_stats(a.cpu().numpy(), b.cpu().numpy())
+    assert s["max_abs"] <= 2 and s["psnr"] >= 50.0, s
