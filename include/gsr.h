@@ -199,6 +199,57 @@ gsr_status gsr_forward_depth_first(int variant, int P, const float* pos, const v
                                    float* conic_opacity, int32_t* ranges, const float* bg_color, uint8_t* out_color,
                                    gsr_stream_t stream);
 
+/* ---- batched forward ------------------------------------------------------ */
+/* No counterpart in the reference, which renders one view per call.  Views
+ * of different scenes and resolutions are rendered by one pass of the
+ * pipeline: one preprocess launch over all views, one radix sort over all
+ * keys (tile ids offset per view), one tile-range pass and one persistent
+ * render launch over every view's tiles.  The per-view parameters are copied
+ * to the device ahead of the kernels, so the kernel sequence of a batch
+ * shape (number of views, largest scene in 256-Gaussian blocks, total tiles,
+ * tile shape, variant) is captured once into a CUDA graph (use_graph != 0,
+ * non-default stream) and replayed for new cameras and outputs. */
+typedef struct {
+    int P;
+    const float* pos;      /* [P,3] */
+    const void* shs;       /* [P,48] f32 or f16 (shs_half) */
+    const float* opacity;  /* [P] */
+    const float* cov3d;    /* [P,6] */
+} gsr_scene_ref;
+
+typedef struct {
+    int scene;             /* index into the scene array */
+    int width, height;
+    float cam_pos[3];      /* host values, as gsr_forward's cam_pos / cam_rot */
+    float cam_rot[9];
+    float focal_x, focal_y, z_far, z_near;
+    float bg[3];
+    uint8_t* out;          /* device [height, width, 3] */
+} gsr_view;
+
+typedef struct gsr_batcher gsr_batcher;
+
+/* Device bytes a batcher allocates at creation (keys, workspace, features,
+ * ranges, parameter blocks); nothing is allocated per batch. */
+size_t gsr_batcher_device_bytes(int max_views, int64_t key_capacity, int64_t max_gaussians, int max_tiles);
+/* NULL on bad sizes or allocation failure.  max_gaussians bounds the sum of
+ * the views' scene sizes in one batch, max_tiles the sum of their tiles. */
+gsr_batcher* gsr_batcher_create(int max_views, int64_t key_capacity, int64_t max_gaussians, int max_tiles);
+void gsr_batcher_destroy(gsr_batcher* b);
+/* Enqueue one batch on `stream` (tile shape 16x16 or 32x16).  Asynchronous;
+ * the images are complete when the stream reaches this point. */
+gsr_status gsr_batcher_render(gsr_batcher* b, int variant, int shs_half, int block_x, int block_y,
+                              const gsr_scene_ref* scenes, int n_scenes, const gsr_view* views, int n_views,
+                              int use_graph, gsr_stream_t stream);
+/* Synchronise `stream` and report the last batch: GSR_OVERFLOW when its keys
+ * exceeded key_capacity (*num_rendered = true count). */
+gsr_status gsr_batcher_finish(gsr_batcher* b, int32_t* num_rendered, gsr_stream_t stream);
+/* Graphs captured so far; device addresses of the batch's key counter and
+ * status word (for asynchronous read-back). */
+int gsr_batcher_graphs(const gsr_batcher* b);
+const int32_t* gsr_batcher_counter(const gsr_batcher* b);
+const uint32_t* gsr_batcher_status(const gsr_batcher* b);
+
 /* ---- stage timing ------------------------------------------------------- */
 /* Profiling hook with no counterpart in the reference.  After
  * gsr_profile_begin(frames), each of the next `frames` gsr_forward calls

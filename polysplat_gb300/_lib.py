@@ -58,6 +58,14 @@ def _declare(L):
                          P, P, sz, P, P, P, P, i64, P, P, P, P, P, P, P], i32),
     }
     sig["gsr_sort_bits_static"] = ([i32, P, i32, P, P, P, P, i64, P], i32)
+    sig["gsr_batcher_device_bytes"] = ([i32, i64, i64, i32], sz)
+    sig["gsr_batcher_create"] = ([i32, i64, i64, i32], P)
+    sig["gsr_batcher_destroy"] = ([P], None)
+    sig["gsr_batcher_render"] = ([P, i32, i32, i32, i32, P, i32, P, i32, i32, P], i32)
+    sig["gsr_batcher_finish"] = ([P, P, P], i32)
+    sig["gsr_batcher_graphs"] = ([P], i32)
+    sig["gsr_batcher_counter"] = ([P], P)
+    sig["gsr_batcher_status"] = ([P], P)
     sig["gsr_depth_first_scratch_size"] = ([i32], sz)
     sig["gsr_forward_depth_first"] = ([i32, i32, P, P, i32, P, P, i32, i32, i32, i32, P, P, f32, f32, f32, f32,
                                        P, P, sz, P, sz, P, P, P, P, i64, P, P, P, P, P, P, P], i32)

@@ -185,6 +185,9 @@ static gsr_status preprocess_params(PreprocessParams& p, int P, const float* pos
         return GSR_INVALID_ARG;
     if (cap > 0 && (!keys || !values)) return GSR_INVALID_ARG;
     p.df = DepthFirstRecords{nullptr, nullptr, nullptr, nullptr};
+    p.gid_base = 0;
+    p.tile_base = 0;
+    p.views = nullptr;
     p.P = P;
     p.pos = pos;
     p.shs = shs;

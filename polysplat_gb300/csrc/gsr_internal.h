@@ -58,11 +58,22 @@ struct PreprocessParams {
     uint32_t* vals;
     long long cap;
     int* counter;
+    // Batches of views (one launch over several views): a view's keys carry
+    // tile ids offset by tile_base and values offset by gid_base; the
+    // per-view parameter blocks live in device memory at `views`.
+    int gid_base;
+    int tile_base;
+    const PreprocessParams* views;
 };
 
 void camera_matrices(int W, int H, const float* pos, const float* rot, float fx, float fy, float zfar, float znear,
                      float* view, float* proj);
 cudaError_t launch_preprocess(const PreprocessParams& p, bool half_sh, cudaStream_t stream);
+// One preprocess (+ large-Gaussian emission) over n_views views whose
+// parameter blocks are in device memory at base.views (shared fields --
+// queue, keys, counter -- are the same in every block and in `base`).
+cudaError_t launch_preprocess_views(const PreprocessParams& base, int n_views, int max_P, bool half_sh,
+                                    cudaStream_t stream);
 // Depth-first pipeline: counting pass (fills p.df, features and the massive
 // queue), then the emission of a Gaussian's pairs at its offset (small
 // rectangles and queued Gaussians separately).
@@ -199,6 +210,22 @@ struct RenderArgs {
     WorkspaceHeader* ws;
 };
 cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream);
+
+// One view of a batched render: its tiles are [tile_base, tile_base +
+// gx * gy) of the batch's global tile ids.
+struct RenderView {
+    int tile_base;
+    int gx;
+    int W, H;
+    float bg[3];
+    int pad;
+    uint8_t* out;  // [H, W, 3]
+};
+// Render every tile of n_views views (view blocks in device memory, sorted
+// by tile_base, views_dev[0].tile_base == 0) in one persistent launch.
+// a.W/a.H are ignored; total_tiles = sum of the views' tile counts.
+cudaError_t launch_render_views(const RenderArgs& a, const RenderView* views_dev, int n_views, int total_tiles,
+                                cudaStream_t stream);
 
 // Depth-first forward (depthfirst.cu): scratch of P-sized arrays, and the
 // pipeline from the counting pass to the tile ranges.  The emitted pair count

@@ -307,9 +307,12 @@ __device__ __forceinline__ void block_flush(Stage& st, const EmitOut& out, int* 
 // pipeline).  COUNT = true: the depth-first pipeline's counting pass -- the
 // same tests, but each Gaussian's number of hit tiles is counted and written
 // with its depth and test geometry instead of keys.
-template <bool HALF, bool COUNT>
-__global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessParams a)
+template <bool HALF, bool COUNT, bool VIEWS>
+__global__ __launch_bounds__(kThreads, 3) void k_preprocess(const __grid_constant__ PreprocessParams a0)
 {
+    // one view per grid row when VIEWS (parameter blocks in device memory)
+    const PreprocessParams& a = VIEWS ? a0.views[blockIdx.y] : a0;
+    const uint32_t view_tag = VIEWS ? (blockIdx.y << 16) : 0u;
     __shared__ uint64_t s_keys[COUNT ? 1 : kWarps][kStage];
     __shared__ uint32_t s_vals[COUNT ? 1 : kWarps][kStage];
     __shared__ int s_fill[kWarps];
@@ -384,8 +387,8 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
         if (COUNT) {
             if (v) s_cnt[warp][lane] = 1u;
         } else {
-            uint64_t key = ((uint64_t)(uint32_t)(rect_min.y * gridx + rect_min.x) << 32) | depth_bits;
-            stage_emit(st, out, v, key, (uint32_t)idx, lane);
+            uint64_t key = ((uint64_t)(uint32_t)(a.tile_base + rect_min.y * gridx + rect_min.x) << 32) | depth_bits;
+            stage_emit(st, out, v, key, (uint32_t)(a.gid_base + idx), lane);
         }
         unsigned m = __ballot_sync(GSR_FULL_MASK, v);
         if (lane == 0 && m) atomicOr(&s_hit[warp], m);
@@ -424,8 +427,9 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
         if (slot >= 0) {
             MassiveEntry e;
             e.ctr_power_depth = make_float4(point_xy.x, point_xy.y, power, p_view.z);
-            e.conic_gid = make_float4(conic.x, conic.y, conic.z, __uint_as_float((uint32_t)idx));
-            e.rect = make_int4(rect_min.x, rect_max.x, rect_min.y, rect_max.y);
+            e.conic_gid = make_float4(conic.x, conic.y, conic.z, __uint_as_float((uint32_t)(a.gid_base + idx)));
+            // x0 < 2^16; the view index rides in the high half
+            e.rect = make_int4((int)((uint32_t)rect_min.x | view_tag), rect_max.x, rect_min.y, rect_max.y);
             a.mq.entries[slot] = e;
             atomicOr(&s_hit[warp], 1u << lane);  // features are written for queued Gaussians
             point_valid = false;
@@ -445,7 +449,7 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
         const int x_hi = __shfl_sync(GSR_FULL_MASK, rect_max.x, i), y_hi = __shfl_sync(GSR_FULL_MASK, rect_max.y, i);
         const uint32_t db = __shfl_sync(GSR_FULL_MASK, depth_bits, i);
         const float pw = __shfl_sync(GSR_FULL_MASK, power, i);
-        const uint32_t gid = (uint32_t)(warp_first + i);
+        const uint32_t gid = (uint32_t)(a.gid_base + warp_first + i);
         for (int y0 = y_lo; y0 < y_hi; y0 += 4) {
             const int y = y0 + ty;
             for (int x0 = x_lo; x0 < x_hi; x0 += 8) {
@@ -455,7 +459,7 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
                     const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
                     if (lane == 0) s_cnt[warp][i] += __popc(m);
                 } else {
-                    uint64_t key = ((uint64_t)(uint32_t)(y * gridx + x) << 32) | db;
+                    uint64_t key = ((uint64_t)(uint32_t)(a.tile_base + y * gridx + x) << 32) | db;
                     stage_emit(st, out, v, key, gid, lane);
                 }
             }
@@ -511,8 +515,8 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const PreprocessPara
             if (COUNT) {
                 if (v) atomicAdd(&s_cnt[warp][owner], 1u);
             } else {
-                uint64_t key = ((uint64_t)(uint32_t)(y * gridx + x) << 32) | db;
-                stage_emit(st, out, v, key, (uint32_t)(warp_first + owner), lane);
+                uint64_t key = ((uint64_t)(uint32_t)(a.tile_base + y * gridx + x) << 32) | db;
+                stage_emit(st, out, v, key, (uint32_t)(a.gid_base + warp_first + owner), lane);
             }
             if (v) atomicOr(&s_hit[warp], 1u << owner);
         }
@@ -624,7 +628,7 @@ __device__ __forceinline__ void sweep_cta(const MassiveEntry& me, const Preproce
     const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
     const float pw = me.ctr_power_depth.z;
     const float3 q = {me.conic_gid.x, me.conic_gid.y, me.conic_gid.z};
-    const int x_lo = me.rect.x, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
+    const int x_lo = me.rect.x & 0xFFFF, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
     const int w = x_hi - x_lo;
     // every thread forms the same band from the same inputs: a uniform branch
     const Band eb = make_band(q, pw, c, 2.0f * (float)max(a.bx, a.by));
@@ -681,7 +685,7 @@ __device__ __forceinline__ void sweep_warp(const MassiveEntry& me, const Preproc
     const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
     const float pw = me.ctr_power_depth.z;
     const float3 q = {me.conic_gid.x, me.conic_gid.y, me.conic_gid.z};
-    const int x_lo = me.rect.x, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
+    const int x_lo = me.rect.x & 0xFFFF, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
     const Band eb = make_band(q, pw, c, 2.0f * (float)max(a.bx, a.by));
     if (eb.ok) {
         for (int r0 = y_lo; r0 < y_hi; r0 += 32) {
@@ -750,8 +754,8 @@ enum : int { kMassiveEmit64 = 0, kMassiveCount = 1, kMassiveEmitDf = 2 };
 // time with all 256 threads, then each warp takes large rectangles on its
 // own.  MODE: emit 64-bit keys, count the hit tiles (depth-first counting
 // pass), or write depth-first pairs at the Gaussian's offset.
-template <int MODE>
-__global__ __launch_bounds__(kThreads) void k_emit_massive(const PreprocessParams a, const DfEmit df)
+template <int MODE, bool VIEWS>
+__global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant__ PreprocessParams a, const DfEmit df)
 {
     __shared__ uint64_t s_keys[MODE == kMassiveEmit64 ? kWarps : 1][kStage];
     __shared__ uint32_t s_vals[MODE == kMassiveEmit64 ? kWarps : 1][kStage];
@@ -782,9 +786,10 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const PreprocessParam
         const MassiveEntry me = a.mq.entries[e];
         const uint32_t db = __float_as_uint(me.ctr_power_depth.w);
         const uint32_t gid = __float_as_uint(me.conic_gid.w);
+        const PreprocessParams& av = VIEWS ? a.views[(uint32_t)me.rect.x >> 16] : a;
         if (MODE == kMassiveEmit64) {
-            sweep_cta(me, a, s_band, lane, warp, [&](bool v, int x, int y) {
-                uint64_t key = ((uint64_t)(uint32_t)(y * a.gx + x) << 32) | db;
+            sweep_cta(me, av, s_band, lane, warp, [&](bool v, int x, int y) {
+                uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + y * av.gx + x) << 32) | db;
                 stage_emit(st, out, v, key, gid, lane);
             });
         } else if (MODE == kMassiveCount) {
@@ -829,9 +834,10 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const PreprocessParam
         const MassiveEntry me = a.mq.entries[a.mq.huge_capacity + e];
         const uint32_t db = __float_as_uint(me.ctr_power_depth.w);
         const uint32_t gid = __float_as_uint(me.conic_gid.w);
+        const PreprocessParams& av = VIEWS ? a.views[(uint32_t)me.rect.x >> 16] : a;
         if (MODE == kMassiveEmit64) {
-            sweep_warp(me, a, lane, [&](bool v, int x, int y) {
-                uint64_t key = ((uint64_t)(uint32_t)(y * a.gx + x) << 32) | db;
+            sweep_warp(me, av, lane, [&](bool v, int x, int y) {
+                uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + y * av.gx + x) << 32) | db;
                 stage_emit(st, out, v, key, gid, lane);
             });
         } else if (MODE == kMassiveCount) {
@@ -988,17 +994,33 @@ static cudaError_t preprocess_common(const PreprocessParams& p, bool half_sh, bo
     }
     const int grid = div_up(p.P, kThreads);
     if (count) {
-        if (half_sh) k_preprocess<true, true><<<grid, kThreads, 0, stream>>>(p);
-        else k_preprocess<false, true><<<grid, kThreads, 0, stream>>>(p);
+        if (half_sh) k_preprocess<true, true, false><<<grid, kThreads, 0, stream>>>(p);
+        else k_preprocess<false, true, false><<<grid, kThreads, 0, stream>>>(p);
     } else {
-        if (half_sh) k_preprocess<true, false><<<grid, kThreads, 0, stream>>>(p);
-        else k_preprocess<false, false><<<grid, kThreads, 0, stream>>>(p);
+        if (half_sh) k_preprocess<true, false, false><<<grid, kThreads, 0, stream>>>(p);
+        else k_preprocess<false, false, false><<<grid, kThreads, 0, stream>>>(p);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.mq.capacity <= 0) return e;
     const DfEmit none{nullptr, nullptr, nullptr, nullptr, 0};
-    if (count) k_emit_massive<kMassiveCount><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, none);
-    else k_emit_massive<kMassiveEmit64><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, none);
+    if (count) k_emit_massive<kMassiveCount, false><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, none);
+    else k_emit_massive<kMassiveEmit64, false><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, none);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_preprocess_views(const PreprocessParams& base, int n_views, int max_P, bool half_sh,
+                                    cudaStream_t stream)
+{
+    if (n_views <= 0 || max_P <= 0) return cudaSuccess;
+    if (n_views > 32767 || !base.views || base.mq.capacity <= 0) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(base.mq.count, 0, kPreprocessRegionBytes, stream);
+    if (e != cudaSuccess) return e;
+    const dim3 grid(div_up(max_P, kThreads), n_views);
+    if (half_sh) k_preprocess<true, false, true><<<grid, kThreads, 0, stream>>>(base);
+    else k_preprocess<false, false, true><<<grid, kThreads, 0, stream>>>(base);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const DfEmit none{nullptr, nullptr, nullptr, nullptr, 0};
+    k_emit_massive<kMassiveEmit64, true><<<device_sm_count() * 4, kThreads, 0, stream>>>(base, none);
     return cudaGetLastError();
 }
 
@@ -1019,7 +1041,7 @@ cudaError_t launch_df_emit_massive(const PreprocessParams& p, const uint32_t* of
     // takes the queue again through the second pair of heads (cleared with
     // the rest of the preprocess region before the counting pass)
     const DfEmit df{offsets, rank, tiles, vals, cap};
-    k_emit_massive<kMassiveEmitDf><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, df);
+    k_emit_massive<kMassiveEmitDf, false><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, df);
     return cudaGetLastError();
 }
 

@@ -49,9 +49,29 @@ struct RenderParams {
     uchar3* out;
     uint32_t* queue;
     uint32_t* status;
+    const RenderView* views;  // batched render: per-view blocks (nullptr: one view)
+    int n_views;
 };
 
 __device__ __forceinline__ uint8_t encode8(float x) { return (uint8_t)fminf(fmaxf(0.0f, x * 255.0f), 255.0f); }
+
+// Final colour of a pixel: C + T' bg with T' = 0 once T < 1e-4; background
+// only for a tile without Gaussians (render.cu:375-394, 1845-1858).
+__device__ __forceinline__ uchar3 encode_px(const float (&c)[3], float t, bool any, float3 bg)
+{
+    if (t < 0.0001f) t = 0.0f;
+    uchar3 o;
+    if (any) {
+        o.x = encode8(c[0] + t * bg.x);
+        o.y = encode8(c[1] + t * bg.y);
+        o.z = encode8(c[2] + t * bg.z);
+    } else {
+        o.x = encode8(bg.x);
+        o.y = encode8(bg.y);
+        o.z = encode8(bg.z);
+    }
+    return o;
+}
 
 // First index in keys[lo, hi) whose tile id is > t (UPPER) or >= t (!UPPER);
 // warp-cooperative 32-way search, log32(n) rounds.
@@ -203,7 +223,7 @@ __device__ __forceinline__ void shade(float (&C)[TY][TX][3], float (&T)[TY][TX],
 }
 
 // RANGE_MODE 0: ranges[] given; 1: warp search in the sorted keys.
-template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA>
+template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA, bool BATCH>
 __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams p)
 {
     constexpr int TX = BX / 8, TY = BY / 4;
@@ -229,8 +249,29 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
 
     int tile = blockIdx.x * kRenderWarps + warp;
     while (tile < p.tiles) {
-        const int ox = (tile % p.gx) * BX;
-        const int oy = (tile / p.gx) * BY;
+        // per-view geometry (batched renders); the single-view kernel reads
+        // its parameters directly
+        int W = 0, H = 0, gx = p.gx, ltile = tile;
+        float3 bg = make_float3(0.f, 0.f, 0.f);
+        uchar3* out = nullptr;
+        if (BATCH) {
+            // the view holding this global tile: last tile_base <= tile
+            int lo = 0, hi = p.n_views - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (__ldg(&p.views[mid].tile_base) <= tile) lo = mid;
+                else hi = mid - 1;
+            }
+            const RenderView& v = p.views[lo];
+            W = v.W;
+            H = v.H;
+            gx = max(1, v.gx);
+            ltile = tile - v.tile_base;
+            bg = make_float3(v.bg[0], v.bg[1], v.bg[2]);
+            out = reinterpret_cast<uchar3*>(v.out);
+        }
+        const int ox = (ltile % gx) * BX;
+        const int oy = (ltile / gx) * BY;
         int start, end;
         if (RANGE_MODE == 0) {
             int2 r = make_int2(0, 0);
@@ -299,20 +340,10 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
 #pragma unroll
             for (int j = 0; j < TX; j++) {
                 const int px = ox + cb + j, py = oy + rb + i;
-                if (px < p.W && py < p.H) {
-                    float t = T[i][j];
-                    if (t < 0.0001f) t = 0.0f;
-                    uchar3 o;
-                    if (total > 0) {
-                        o.x = encode8(C[i][j][0] + t * p.bg.x);
-                        o.y = encode8(C[i][j][1] + t * p.bg.y);
-                        o.z = encode8(C[i][j][2] + t * p.bg.z);
-                    } else {
-                        o.x = encode8(p.bg.x);
-                        o.y = encode8(p.bg.y);
-                        o.z = encode8(p.bg.z);
-                    }
-                    p.out[(size_t)py * p.W + px] = o;
+                if (BATCH) {
+                    if (px < W && py < H) out[(size_t)py * W + px] = encode_px(C[i][j], T[i][j], total > 0, bg);
+                } else {
+                    if (px < p.W && py < p.H) p.out[(size_t)py * p.W + px] = encode_px(C[i][j], T[i][j], total > 0, p.bg);
                 }
             }
         int next = 0;
@@ -328,10 +359,10 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
     }
 }
 
-template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA>
+template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA, bool BATCH = false>
 cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
 {
-    auto kern = k_render<BX, BY, CADENCE, SHADER, DT, RANGE_MODE, TMA>;
+    auto kern = k_render<BX, BY, CADENCE, SHADER, DT, RANGE_MODE, TMA, BATCH>;
     static int per_sm = 0;
     if (per_sm == 0) {
         int b = 0;
@@ -379,7 +410,25 @@ cudaError_t dispatch_shape(int variant, bool tma, const RenderParams& p, cudaStr
     }
 }
 
+// Batched renders: ranges always precomputed, TMA staging (the batch's own
+// feature buffers are aligned), 16x16 and 32x16 tiles.
+template <int BX, int BY>
+cudaError_t dispatch_batch(int variant, const RenderParams& p, cudaStream_t stream)
+{
+    constexpr int SH = (BX == 16 && BY == 16) ? 0 : 1;
+    switch (variant) {
+    case GSR_RENDER_PERSISTENT_RANGES: return launch_variant<BX, BY, 8, 0, false, 0, true, true>(p, stream);
+    case GSR_RENDER_PERSISTENT_FUSED: return launch_variant<BX, BY, 16, 0, false, 0, true, true>(p, stream);
+    case GSR_RENDER_DEFAULT:
+    case GSR_RENDER_RANGES_CADENCE2: return launch_variant<BX, BY, 2, SH, false, 0, true, true>(p, stream);
+    case GSR_RENDER_DT: return launch_variant<BX, BY, 8, 0, true, 0, true, true>(p, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 }  // namespace
+
+static cudaError_t launch_prepared(const RenderArgs& a, RenderParams& p, cudaStream_t stream);
 
 cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream)
 {
@@ -402,12 +451,51 @@ cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream)
     p.out = reinterpret_cast<uchar3*>(a.out);
     p.queue = &a.ws->render_queue;
     p.status = &a.ws->status;
+    p.views = nullptr;
+    p.n_views = 0;
+    return launch_prepared(a, p, stream);
+}
+
+cudaError_t launch_render_views(const RenderArgs& a, const RenderView* views_dev, int n_views, int total_tiles,
+                                cudaStream_t stream)
+{
+    if (!views_dev || n_views <= 0) return cudaErrorInvalidValue;
+    RenderParams p;
+    p.n_host = a.num;
+    p.d_num = a.d_num;
+    p.cap = a.d_num ? a.cap : (long long)a.num;
+    p.W = p.H = p.gx = 1;  // per view
+    p.tiles = total_tiles;
+    p.P = a.P;
+    p.xy = a.xy;
+    p.rgbd = a.rgbd;
+    p.con = a.con;
+    p.keys = a.keys;
+    p.vals = a.vals;
+    p.ranges = a.ranges;
+    p.bg = make_float3(0.f, 0.f, 0.f);
+    p.out = nullptr;
+    p.queue = &a.ws->render_queue;
+    p.status = &a.ws->status;
+    p.views = views_dev;
+    p.n_views = n_views;
+    return launch_prepared(a, p, stream);
+}
+
+static cudaError_t launch_prepared(const RenderArgs& a, RenderParams& p, cudaStream_t stream)
+{
     if (p.tiles <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(p.queue, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
     // TMA bulk copies need 16-byte aligned feature arrays.
     const bool tma = ((reinterpret_cast<uintptr_t>(a.xy) | reinterpret_cast<uintptr_t>(a.rgbd) |
                        reinterpret_cast<uintptr_t>(a.con)) & 15u) == 0;
+    if (p.views) {
+        if (!tma || !p.ranges) return cudaErrorInvalidValue;
+        if (a.bx == 16 && a.by == 16) return dispatch_batch<16, 16>(a.variant, p, stream);
+        if (a.bx == 32 && a.by == 16) return dispatch_batch<32, 16>(a.variant, p, stream);
+        return cudaErrorInvalidValue;
+    }
     if (a.bx == 16 && a.by == 16) return dispatch_shape<16, 16>(a.variant, tma, p, stream);
     if (a.bx == 32 && a.by == 16) return dispatch_shape<32, 16>(a.variant, tma, p, stream);
     if (a.bx == 24 && a.by == 16) return dispatch_shape<24, 16>(a.variant, tma, p, stream);
