@@ -25,6 +25,7 @@ cores.  Multi-GPU: replicas only (one independent renderer per rank).
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -44,7 +45,9 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="plain_3m_1080p")
+    ap.add_argument("--workload", default="serve_mix",
+                    help="serve_mix (config 3, the headline), or a plain-forward workload: plain_3m_1080p, "
+                         "plain_100k_800x600, clustered_1m_1080p, city_20m_8k")
     ap.add_argument("--impl", default="gsr", choices=["gsr", "reference", "reference-gpu"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true",
@@ -159,6 +162,21 @@ def run_reference(args):
         return 0
     from polysplat_gb300 import scenes
 
+    if args.workload == "serve_mix":
+        # the request stream in order on the host cores (the reference has
+        # no CPU path: its algorithm restated in FP64), bounded to about a minute
+        raws, reqs = scenes.serve_mix()
+        cpu = serve_cpu_baseline(raws, reqs[: max(1, args.steps)], seconds=60.0)
+        line = {"impl": "reference", "metric": "frames/s", "value": cpu["value"], "unit": "frames/s",
+                "n_gpus": world, "steps": cpu["requests"], "warmup": 0,
+                "ms_per_step": 1000.0 / cpu["value"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "serve_mix", "scenes_gaussians": [r.num for r in raws],
+                           "requests": len(reqs)},
+                "cpu_baseline": cpu,
+                "e2e": {"value": cpu["value"], "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
     raw, cams = scenes.workload(args.workload)
     cam = cams[0]
     from oracle import oracle as O
@@ -188,9 +206,6 @@ def run_reference(args):
 
 # ----------------------------------------------------------------------------- GPU arm
 def run_gsr(args):
-    import ctypes
-
-    import numpy as np
     import torch
 
     rank, world, local = dist_env()
@@ -202,6 +217,25 @@ def run_gsr(args):
         dist.init_process_group("nccl", rank=rank, world_size=world)
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.workload == "serve_mix":
+        line = run_serve(args, dev, rank, world, dist)
+    else:
+        line = forward_line(args, dev, rank, world, dist)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def forward_line(args, dev, rank, world, dist):
+    """The plain forward of one workload: device-timed frames/s, stage times,
+    roofline, e2e through the public API, CPU and reference-GPU arms."""
+    import ctypes
+
+    import numpy as np
+    import torch
 
     from polysplat_gb300 import Camera, Rasterizer, Scene, ops, scenes
     from polysplat_gb300._lib import check, lib
@@ -264,7 +298,7 @@ def run_gsr(args):
     K = args.steps
     check(L.gsr_profile_begin(K), "profile_begin")
 
-    sampler = ClockSampler(local)
+    sampler = ClockSampler(dev.index or 0)
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -402,11 +436,130 @@ def run_gsr(args):
                 "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": 60,
                         "d2h_bytes_per_step": cam.width * cam.height * 3 + 4},
                 "gpu_launches": launches_per_frame * K, "clocks": clocks}
-        print(json.dumps(line), flush=True)
+    return line
+
+
+def run_serve(args, dev, rank, world, dist):
+    """Config 3: resident scenes of 0.5/2/5/10 M Gaussians, 512 requests
+    arriving by a Poisson process at 240/s, resolutions 720p-2160p, 60 GB
+    admission budget.  The plain per-request forward against the served,
+    continuously batched path (tuned by the autotuner on a 128-request
+    sample), both saturated (all requests queued at once: capacity) and in
+    real time (latency).  `value` is the served capacity with every image
+    delivered to pinned host memory."""
+    import gc
+
+    import torch
+
+    from polysplat_gb300 import Scene, scenes
+    from polysplat_gb300.serving import PlainServer, Server, autotune
+
+    budget = 60 << 30
+    raws, reqs = scenes.serve_mix()
+    scs = [Scene.from_raw(r, dev) for r in raws]
+    torch.cuda.synchronize()
+    sampler = ClockSampler(dev.index or 0)
+
+    # plain per-request forward (the reference's usage of Rasterizer.forward)
+    plain = PlainServer(scs, 1 << 28, dev)
+    plain.run(reqs[:16], realtime=False)
+    p_sat, _ = plain.run(reqs, realtime=False)
+    p_rt, _ = plain.run(reqs, realtime=True)
+    del plain
+    gc.collect()
+    torch.cuda.empty_cache()
+
+    log = (lambda m: print(m, file=sys.stderr, flush=True)) if rank == 0 else None
+    best, table = autotune(scs, reqs[:128], dev, budget_bytes=budget, log=log)
+    srv = Server(scs, dev, budget, best)
+    st = srv.run(reqs[: max(3, args.warmup) * 16], realtime=False, deliver=True)  # warm-up: graphs, pinned pool
+    for r in reqs:
+        srv.release(r)
     if dist is not None:
         dist.barrier()
-        dist.destroy_process_group()
-    return 0
+    sampler.start()
+    s_sat = srv.run(reqs, realtime=False, deliver=True)
+    for r in reqs:
+        srv.release(r)
+    s_rt = srv.run(reqs, realtime=True, deliver=True)
+    for r in reqs:
+        srv.release(r)
+    clocks = sampler.stop()
+    s_dev = srv.run(reqs, realtime=False, deliver=False)
+    srv.close()
+    del srv
+    gc.collect()
+    torch.cuda.empty_cache()
+
+    # the plain forward of config 1 on the same GPU: stage times and the
+    # roofline of its dominant kernel
+    fargs = argparse.Namespace(**vars(args))
+    fargs.workload, fargs.steps, fargs.quick, fargs.no_cpu_baseline = "plain_3m_1080p", 200, False, True
+    fwd = forward_line(fargs, dev, rank, world, dist)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = serve_cpu_baseline(raws, reqs, seconds=15.0)
+    wall = s_sat.wall_s
+    if dist is not None:
+        t = torch.tensor([wall], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        wall = float(t.item())
+    value = world * len(reqs) / wall
+    img_bytes = sum(r.camera.width * r.camera.height * 3 for r in reqs) / len(reqs)
+    # kernel launches of the saturated run: small batches (preprocess, large-
+    # Gaussian emission, upsweep, 6 digit passes, ranges, render) and large
+    # frames (20 launches of the depth-first forward)
+    launches = s_sat.batches * 11 + s_sat.large * 20
+    if rank != 0:
+        return None
+    return {"metric": "frames/s", "value": value, "unit": "frames/s", "n_gpus": world, "steps": len(reqs),
+            "warmup": max(3, args.warmup), "ms_per_step": 1000.0 * wall / len(reqs), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "serve_mix", "scenes_gaussians": [r.num for r in raws], "requests": len(reqs),
+                       "arrival": "Poisson 240/s", "resolutions": ["1280x720", "1920x1080", "2560x1440",
+                                                                   "3840x2160"],
+                       "budget_gb": 60, "tuned": dataclasses.asdict(best), "sh": "fp16",
+                       "l2": "scenes of 0.5-10 M Gaussians (68 MB-1.4 GB), larger than L2",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "served": {"saturated": s_sat.as_dict(), "realtime_240hz": s_rt.as_dict(),
+                       "saturated_device_only": s_dev.as_dict()},
+            "plain": {"saturated": p_sat.as_dict(), "realtime_240hz": p_rt.as_dict()},
+            "speedup_vs_plain": {"saturated_frames_per_s": s_sat.frames_per_s / p_sat.frames_per_s,
+                                 "realtime_p99": p_rt.p99_ms / s_rt.p99_ms},
+            "autotune": [{"config": c, "frames_per_s": f} for c, f in table],
+            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 376,
+                    "d2h_bytes_per_step": int(img_bytes)},
+            "roofline": dict(fwd["roofline"], workload="plain_3m_1080p (config 1 forward)") if fwd else None,
+            "forward": {k: fwd[k] for k in ("value", "ms_per_step", "stages_ms", "e2e", "reference_gpu", "config")}
+            if fwd else None,
+            "cpu_baseline": cpu,
+            "gpu_launches": launches, "clocks": clocks}
+
+
+def serve_cpu_baseline(raws, reqs, seconds: float):
+    """The FP64 oracle on the host cores, rendering the request stream in
+    order for about `seconds` (at least one request)."""
+    from oracle import oracle as O
+    from polysplat_gb300.rasterizer import Camera
+
+    threads = O.nthreads_default()
+    prepared = {}
+    n, t0 = 0, time.perf_counter()
+    for r in reqs:
+        if r.scene not in prepared:
+            raw = raws[r.scene]
+            prepared[r.scene] = O.scene_transform(raw.log_scales, raw.quats, raw.opacity_logits)
+        op, cov = prepared[r.scene]
+        raw = raws[r.scene]
+        O.forward(raw.means, raw.shs, op, cov, r.camera, cadence=16, half_sh=True, nthreads=threads)
+        n += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    el = time.perf_counter() - t0
+    return {"value": n / el, "unit": "frames/s", "cores": threads, "kind": "port", "requests": n, "seconds": el,
+            "sample": "the first %d requests of the serve_mix stream in %.1f s (FP64 oracle, %d threads; scene "
+                      "transforms included)" % (n, el, threads)}
 
 
 def run_reference_gpu(args):

@@ -236,7 +236,7 @@ size_t gsr_batcher_device_bytes(int max_views, int64_t key_capacity, int64_t max
  * the views' scene sizes in one batch, max_tiles the sum of their tiles. */
 gsr_batcher* gsr_batcher_create(int max_views, int64_t key_capacity, int64_t max_gaussians, int max_tiles);
 void gsr_batcher_destroy(gsr_batcher* b);
-/* Enqueue one batch on `stream` (tile shape 16x16 or 32x16).  Asynchronous;
+/* Enqueue one batch on `stream` (tile shape 16x16, 32x16 or 32x32).  Asynchronous;
  * the images are complete when the stream reaches this point. */
 gsr_status gsr_batcher_render(gsr_batcher* b, int variant, int shs_half, int block_x, int block_y,
                               const gsr_scene_ref* scenes, int n_scenes, const gsr_view* views, int n_views,
@@ -247,6 +247,11 @@ gsr_status gsr_batcher_finish(gsr_batcher* b, int32_t* num_rendered, gsr_stream_
 /* Graphs captured so far; device addresses of the batch's key counter and
  * status word (for asynchronous read-back). */
 int gsr_batcher_graphs(const gsr_batcher* b);
+/* Dispatch thresholds of the tile-key emission, in tiles of a Gaussian's
+ * rectangle: from massive_area (default 32) on, a rectangle is queued for the
+ * large-Gaussian kernel; from huge_area (default 2048) on, a whole CTA sweeps
+ * it.  They change which scheme tests the tiles, never the keys. */
+gsr_status gsr_batcher_set_thresholds(gsr_batcher* b, int massive_area, int huge_area);
 const int32_t* gsr_batcher_counter(const gsr_batcher* b);
 const uint32_t* gsr_batcher_status(const gsr_batcher* b);
 

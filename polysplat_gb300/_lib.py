@@ -64,6 +64,7 @@ def _declare(L):
     sig["gsr_batcher_render"] = ([P, i32, i32, i32, i32, P, i32, P, i32, i32, P], i32)
     sig["gsr_batcher_finish"] = ([P, P, P], i32)
     sig["gsr_batcher_graphs"] = ([P], i32)
+    sig["gsr_batcher_set_thresholds"] = ([P, i32, i32], i32)
     sig["gsr_batcher_counter"] = ([P], P)
     sig["gsr_batcher_status"] = ([P], P)
     sig["gsr_depth_first_scratch_size"] = ([i32], sz)

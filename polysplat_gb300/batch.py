@@ -68,6 +68,10 @@ class Batcher:
         except Exception:
             pass
 
+    def set_thresholds(self, massive_area: int, huge_area: int) -> None:
+        """Dispatch thresholds of the tile-key emission (tiles of a rectangle)."""
+        check(lib().gsr_batcher_set_thresholds(self._h, int(massive_area), int(huge_area)), "batcher_set_thresholds")
+
     @property
     def graphs(self) -> int:
         return int(lib().gsr_batcher_graphs(self._h))

@@ -67,6 +67,8 @@ struct gsr_batcher {
     std::map<gsr::Shape, int> seen;
     std::mutex mu;
     int last_total = 0;
+    int massive_area = gsr::kDefaultMassiveArea;
+    int huge_area = gsr::kDefaultHugeArea;
 };
 
 namespace gsr {
@@ -93,7 +95,7 @@ Sizes sizes_of(int max_views, long long cap, long long max_g, int max_tiles)
     return s;
 }
 
-bool valid_shape(int bx, int by) { return (bx == 16 && by == 16) || (bx == 32 && by == 16); }
+bool valid_shape(int bx, int by) { return (bx == 16 && by == 16) || (bx == 32 && by == 16) || (bx == 32 && by == 32); }
 
 // Fill the parameter block of one view (the same fields the single-view
 // preprocess entry fills), plus its offsets into the batch.
@@ -139,6 +141,9 @@ void pack_view(PreprocessParams& p, const gsr_scene_ref& sc, const gsr_view& v, 
     p.gid_base = gid_base;
     p.tile_base = tile_base;
     p.views = b->d_pre;
+    p.n_views = 0;  // set per batch in the base block
+    p.massive_area = b->massive_area;
+    p.huge_area = b->huge_area;
 }
 
 // The kernel sequence of a batch (everything after the parameter copy).
@@ -161,6 +166,7 @@ cudaError_t enqueue(gsr_batcher* b, const Shape& s, int max_P, cudaStream_t st)
     base.cap = b->cap;
     base.counter = b->counter;
     base.views = b->d_pre;
+    base.n_views = s.n_views;
     base.bx = s.bx;
     base.by = s.by;
     e = launch_preprocess_views(base, s.n_views, max_P, s.half != 0, st);
@@ -377,6 +383,15 @@ gsr_status gsr_batcher_finish(gsr_batcher* b, int32_t* num_rendered, gsr_stream_
 }
 
 int gsr_batcher_graphs(const gsr_batcher* b) { return b ? (int)b->graphs.size() : 0; }
+
+gsr_status gsr_batcher_set_thresholds(gsr_batcher* b, int massive_area, int huge_area)
+{
+    if (!b || massive_area < 2 || huge_area < massive_area) return GSR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(b->mu);
+    b->massive_area = massive_area;
+    b->huge_area = huge_area;
+    return GSR_OK;
+}
 
 const int32_t* gsr_batcher_counter(const gsr_batcher* b) { return b ? b->counter : nullptr; }
 

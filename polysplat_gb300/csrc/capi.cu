@@ -188,6 +188,9 @@ static gsr_status preprocess_params(PreprocessParams& p, int P, const float* pos
     p.gid_base = 0;
     p.tile_base = 0;
     p.views = nullptr;
+    p.n_views = 0;
+    p.massive_area = kDefaultMassiveArea;
+    p.huge_area = kDefaultHugeArea;
     p.P = P;
     p.pos = pos;
     p.shs = shs;

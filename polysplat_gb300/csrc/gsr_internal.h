@@ -64,7 +64,13 @@ struct PreprocessParams {
     int gid_base;
     int tile_base;
     const PreprocessParams* views;
+    int n_views;  // entries at `views`
+    // dispatch thresholds of the multi-tile emission (tiles of the rectangle)
+    int massive_area;
+    int huge_area;
 };
+constexpr int kDefaultMassiveArea = 32;
+constexpr int kDefaultHugeArea = 2048;
 
 void camera_matrices(int W, int H, const float* pos, const float* rot, float fx, float fy, float zfar, float znear,
                      float* view, float* proj);

@@ -242,7 +242,7 @@ __device__ __forceinline__ void stage_flush(Stage& s, const EmitOut& o, unsigned
     base = __shfl_sync(GSR_FULL_MASK, base, 0);
     for (int i = lane; i < s.fill; i += 32) {
         long long pos = (long long)base + i;
-        if (pos < o.cap) {
+        if (pos >= 0 && pos < o.cap) {  // a counter past 2^31 wraps: never write below the buffer
             o.keys[pos] = s.k[i];
             o.vals[pos] = s.v[i];
         }
@@ -266,10 +266,11 @@ __device__ __forceinline__ void stage_emit(Stage& s, const EmitOut& o, bool vali
     s.fill += n;
 }
 
-// Tile rectangles at least this large are queued for k_emit_massive.
-constexpr int kMassiveArea = 32;
-// Rectangles of at least this many tiles are swept by a whole CTA.
-constexpr int kHugeArea = 2048;
+// Dispatch thresholds (PreprocessParams::massive_area / huge_area; the
+// defaults are kDefaultMassiveArea / kDefaultHugeArea): tile rectangles at
+// least massive_area tiles large are queued for k_emit_massive, and of those
+// the ones of at least huge_area tiles are swept by a whole CTA.  They only
+// decide which scheme tests a rectangle's tiles, never which keys come out.
 
 // Block-wide final flush of every warp's staged keys with one atomic per CTA.
 __device__ __forceinline__ void block_flush(Stage& st, const EmitOut& out, int* s_fill, long long* s_base,
@@ -295,7 +296,7 @@ __device__ __forceinline__ void block_flush(Stage& st, const EmitOut& out, int* 
     const long long wb = s_base[warp];
     for (int i = lane; i < st.fill; i += 32) {
         long long pos = wb + i;
-        if (pos < out.cap) {
+        if (pos >= 0 && pos < out.cap) {
             out.keys[pos] = st.k[i];
             out.vals[pos] = st.v[i];
         }
@@ -395,18 +396,18 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const __grid_constan
     }
     point_valid = point_valid && !single;
 
-    // (2) multi-tile Gaussians.  Rectangles of at least kMassiveArea tiles go
+    // (2) multi-tile Gaussians.  Rectangles of at least massive_area tiles go
     // to the massive queue, where a whole CTA tests them (k_emit_massive);
     // the rest form one flattened task pool per warp (the reference's
     // "fragmented" scheme, preprocess.cu:521-623).  If the queue is full, the
     // warp tests the Gaussian itself over an 8x4 tile window (the reference's
     // "massive" scheme, preprocess.cu:444-519).  Every scheme tests every
     // tile of the rectangle with the same test, so the key set is the same.
-    bool massive = point_valid && area >= kMassiveArea;
+    bool massive = point_valid && area >= a.massive_area;
     {
         // huge rectangles first try the CTA-swept region, then the warp one
         int slot = -1;
-        const bool want_huge = massive && area >= kHugeArea;
+        const bool want_huge = massive && area >= a.huge_area;
         const unsigned mh = __ballot_sync(GSR_FULL_MASK, want_huge);
         if (mh) {
             int base = 0;
@@ -786,6 +787,7 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
         const MassiveEntry me = a.mq.entries[e];
         const uint32_t db = __float_as_uint(me.ctr_power_depth.w);
         const uint32_t gid = __float_as_uint(me.conic_gid.w);
+        if (VIEWS && ((uint32_t)me.rect.x >> 16) >= (uint32_t)a.n_views) continue;
         const PreprocessParams& av = VIEWS ? a.views[(uint32_t)me.rect.x >> 16] : a;
         if (MODE == kMassiveEmit64) {
             sweep_cta(me, av, s_band, lane, warp, [&](bool v, int x, int y) {
@@ -834,6 +836,7 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
         const MassiveEntry me = a.mq.entries[a.mq.huge_capacity + e];
         const uint32_t db = __float_as_uint(me.ctr_power_depth.w);
         const uint32_t gid = __float_as_uint(me.conic_gid.w);
+        if (VIEWS && ((uint32_t)me.rect.x >> 16) >= (uint32_t)a.n_views) continue;
         const PreprocessParams& av = VIEWS ? a.views[(uint32_t)me.rect.x >> 16] : a;
         if (MODE == kMassiveEmit64) {
             sweep_warp(me, av, lane, [&](bool v, int x, int y) {

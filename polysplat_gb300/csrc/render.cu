@@ -411,7 +411,7 @@ cudaError_t dispatch_shape(int variant, bool tma, const RenderParams& p, cudaStr
 }
 
 // Batched renders: ranges always precomputed, TMA staging (the batch's own
-// feature buffers are aligned), 16x16 and 32x16 tiles.
+// feature buffers are aligned), 16x16, 32x16 and 32x32 tiles.
 template <int BX, int BY>
 cudaError_t dispatch_batch(int variant, const RenderParams& p, cudaStream_t stream)
 {
@@ -494,6 +494,7 @@ static cudaError_t launch_prepared(const RenderArgs& a, RenderParams& p, cudaStr
         if (!tma || !p.ranges) return cudaErrorInvalidValue;
         if (a.bx == 16 && a.by == 16) return dispatch_batch<16, 16>(a.variant, p, stream);
         if (a.bx == 32 && a.by == 16) return dispatch_batch<32, 16>(a.variant, p, stream);
+        if (a.bx == 32 && a.by == 32) return dispatch_batch<32, 32>(a.variant, p, stream);
         return cudaErrorInvalidValue;
     }
     if (a.bx == 16 && a.by == 16) return dispatch_shape<16, 16>(a.variant, tma, p, stream);

@@ -1,0 +1,449 @@
+"""Serving: render requests over resident scenes with continuous batching.
+
+No counterpart in the reference, which renders one view per call.  A server
+keeps several scenes resident on the device and renders a stream of
+requests (scene, camera, resolution) as they arrive.
+
+* Two lanes, on their own CUDA streams.
+  - The small lane batches requests of modest key count and renders each
+    batch with one pass of the pipeline (``Batcher``; a CUDA graph per batch
+    shape, replayed).
+  - The large lane renders one big request at a time with the depth-first
+    forward, which sorts 32-bit tile ids in 2 passes instead of 64-bit keys
+    in 5-6.
+  Small requests never queue behind a big one, and the work of both lanes
+  overlaps on the device.
+* Admission is continuous: a request that arrives while others are on the
+  GPU joins the next batch of its lane as soon as a buffer set of that lane
+  is free.  Every buffer set is allocated once, at start-up, within the
+  memory budget; a request is only admitted into a buffer set whose key
+  capacity covers its estimated key count.  The estimate is learned per
+  scene from the key counts of finished work.  A request whose keys
+  overflowed is put back with a doubled estimate.
+* ``PlainServer`` is the baseline: one ``Rasterizer.forward`` per request in
+  arrival order, with a host synchronisation per frame.
+* ``autotune`` picks the tile shape, the batch depth, the lane threshold
+  and the emission dispatch thresholds by timing candidates on a sample of
+  the request stream.
+"""
+from __future__ import annotations
+
+import collections
+import ctypes
+import dataclasses
+import math
+import time
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib as R
+from . import ops
+from ._lib import GsrError, lib
+from .batch import Batcher, View
+from .rasterizer import E2E, Camera, Rasterizer
+
+
+@dataclasses.dataclass
+class TuneConfig:
+    block_x: int = 16
+    block_y: int = 16
+    max_views: int = 8          # batch depth of the small lane
+    large_keys: int = 8_000_000  # requests estimated at or above this key count take the large lane
+    massive_area: int = 32      # emission dispatch thresholds (tiles of a Gaussian's rectangle)
+    huge_area: int = 2048
+    variant: int = R.RENDER_PERSISTENT_FUSED
+
+
+@dataclasses.dataclass
+class RunStats:
+    frames_per_s: float
+    p50_ms: float
+    p99_ms: float
+    p99_1080p_ms: float
+    wall_s: float
+    requests: int
+    batches: int = 0
+    mean_batch: float = 0.0
+    large: int = 0
+    retries: int = 0
+
+    def as_dict(self):
+        return dataclasses.asdict(self)
+
+
+def _stats(lat_s: Sequence[float], widths: Sequence[int], wall: float, **kw) -> RunStats:
+    lat = np.asarray(lat_s) * 1000.0
+    w = np.asarray(widths)
+    hd = lat[w == 1920] if len(lat) else lat
+    return RunStats(frames_per_s=len(lat) / wall if wall > 0 else 0.0,
+                    p50_ms=float(np.percentile(lat, 50)) if len(lat) else math.nan,
+                    p99_ms=float(np.percentile(lat, 99)) if len(lat) else math.nan,
+                    p99_1080p_ms=float(np.percentile(hd, 99)) if len(hd) else math.nan,
+                    wall_s=wall, requests=len(lat), **kw)
+
+
+class _DevWord:
+    """A torch view of a device word owned by the C library."""
+
+    def __init__(self, ptr: int, dtype: str, device):
+        self.__cuda_array_interface__ = {"shape": (1,), "typestr": dtype, "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+        self.device = device
+
+    def tensor(self) -> torch.Tensor:
+        return torch.as_tensor(self, device=self.device)
+
+
+def _pixels(cam) -> int:
+    return int(cam.width) * int(cam.height)
+
+
+class KeyEstimator:
+    """Keys per pixel of each scene, learned from finished frames (the
+    largest rate seen, so an estimate errs high)."""
+
+    def __init__(self, scenes):
+        # start from about 2.5 keys per pixel per million Gaussians
+        self.rate = [2.5e-6 * max(1, s.num_vertex) for s in scenes]
+
+    def __call__(self, scene: int, cam) -> int:
+        return int(self.rate[scene] * _pixels(cam)) + 4096
+
+    def observe(self, scene: int, cam, keys: float) -> None:
+        r = keys / max(1, _pixels(cam))
+        self.rate[scene] = max(self.rate[scene] * 0.98, r)
+
+    def observe_batch(self, items: Sequence[Tuple[int, object]], keys: int) -> None:
+        est = [self(s, c) for s, c in items]
+        tot = max(1, sum(est))
+        for (s, c), e in zip(items, est):
+            self.observe(s, c, keys * e / tot)
+
+
+# ----------------------------------------------------------------------------- plain baseline
+class PlainServer:
+    """One forward per request in arrival order (the reference's usage of
+    ``Rasterizer.forward``): a key count read-back and a host
+    synchronisation per frame."""
+
+    def __init__(self, scenes, key_capacity: int, device, bg=(0.0, 0.0, 0.0)):
+        self.scenes = scenes
+        self.device = device
+        self.bg = torch.tensor(list(bg), dtype=torch.float32)
+        # one key buffer set shared by all scenes (features sized for the largest)
+        big = max(scenes, key=lambda s: s.num_vertex)
+        self.rast = Rasterizer(big, key_capacity, 1 << 17)
+
+    def render(self, req) -> torch.Tensor:
+        cam = Camera.from_spec(req.camera)
+        return self.rast.forward(self.scenes[req.scene], cam, self.bg, render_variant=E2E)
+
+    def run(self, reqs, realtime: bool = True, keep: bool = False):
+        lat, widths, images = [], [], []
+        t0 = time.perf_counter()
+        for r in reqs:
+            if realtime:
+                while time.perf_counter() - t0 < r.arrival_s:
+                    pass
+            img = self.render(r)
+            torch.cuda.current_stream(self.device).synchronize()
+            if keep:
+                images.append(img.clone())
+            done = time.perf_counter() - t0
+            lat.append(done - (r.arrival_s if realtime else 0.0))
+            widths.append(r.camera.width)
+        wall = time.perf_counter() - t0 - (reqs[0].arrival_s if realtime and reqs else 0.0)
+        return _stats(lat, widths, wall), images
+
+
+# ----------------------------------------------------------------------------- lanes
+class _LargeSlot:
+    """Buffers of one depth-first frame (allocated once)."""
+
+    def __init__(self, key_capacity: int, max_P: int, device):
+        n = key_capacity
+        self.cap = n
+        self.tiles_u = torch.empty(n, dtype=torch.int32, device=device)
+        self.tiles_s = torch.empty(n, dtype=torch.int32, device=device)
+        self.vals_u = torch.empty(n, dtype=torch.int32, device=device)
+        self.vals_s = torch.empty(n, dtype=torch.int32, device=device)
+        self.ws = torch.zeros(ops.get_sort_buffer_size(n), dtype=torch.int8, device=device)
+        self.scratch = torch.zeros(ops.depth_first_scratch_size(max_P), dtype=torch.int8, device=device)
+        self.xy = torch.empty((max_P, 2), dtype=torch.float32, device=device)
+        self.rgbd = torch.empty((max_P, 4), dtype=torch.float32, device=device)
+        self.con = torch.empty((max_P, 4), dtype=torch.float32, device=device)
+        self.ranges = torch.empty((1 << 17, 2), dtype=torch.int32, device=device)
+        self.counter = torch.zeros(1, dtype=torch.int32, device=device)
+        self.host = torch.zeros(2, dtype=torch.int32, pin_memory=True)  # key count, status word
+        self.event = torch.cuda.Event()
+        self.stream = torch.cuda.Stream(device)  # frames of different slots overlap on the device
+        self.job = None
+
+    @staticmethod
+    def device_bytes(key_capacity: int, max_P: int) -> int:
+        return (16 * key_capacity + int(ops.get_sort_buffer_size(key_capacity))
+                + int(ops.depth_first_scratch_size(max_P)) + 40 * max_P + (1 << 20))
+
+
+class Server:
+    """Continuous-batching server over resident scenes (see module doc)."""
+
+    def __init__(self, scenes, device, budget_bytes: int = 60 << 30, config: Optional[TuneConfig] = None,
+                 small_slots: int = 2, large_slots: int = 2, bg=(0.0, 0.0, 0.0)):
+        self.scenes = scenes
+        self.device = torch.device(device)
+        self.cfg = config or TuneConfig()
+        self.bg = [float(x) for x in bg]
+        self.est = KeyEstimator(scenes)
+        cfg = self.cfg
+        max_P = max(s.num_vertex for s in scenes)
+        # buffer sets, sized within the budget: large lane first (one 4K frame
+        # of the largest scene), the small lane from what is left
+        large_cap = 1 << 28
+        while large_slots * _LargeSlot.device_bytes(large_cap, max_P) > budget_bytes // 2 and large_cap > (1 << 22):
+            large_cap //= 2
+        self.large = [_LargeSlot(large_cap, max_P, self.device) for _ in range(large_slots)]
+        left = budget_bytes - large_slots * _LargeSlot.device_bytes(large_cap, max_P)
+        tiles_4k = ((3840 + cfg.block_x - 1) // cfg.block_x) * ((2160 + cfg.block_y - 1) // cfg.block_y)
+        max_g = min((1 << 31) - 1, cfg.max_views * max_P)
+        small_cap = 1 << 26
+        while small_cap > (1 << 20) and small_slots * Batcher.device_bytes(cfg.max_views, small_cap, max_g,
+                                                                          cfg.max_views * tiles_4k) > left:
+            small_cap //= 2
+        self.small_cap = small_cap
+        self.small = []
+        for _ in range(small_slots):
+            b = Batcher(cfg.max_views, small_cap, max_g, cfg.max_views * tiles_4k, self.device)
+            b.set_thresholds(cfg.massive_area, cfg.huge_area)
+            ctr = _DevWord(b.counter_ptr(), "<i4", self.device).tensor()
+            self.small.append({"b": b, "ctr": ctr, "host": torch.zeros(1, dtype=torch.int32, pin_memory=True),
+                               "event": torch.cuda.Event(), "job": None})
+        self.s_small = torch.cuda.Stream(self.device)
+        self.max_g = max_g
+        self.tiles_cap = cfg.max_views * tiles_4k
+        self.deliver = False
+        self._pinned: Dict[Tuple[int, int], List[torch.Tensor]] = collections.defaultdict(list)
+
+    # -- delivery of results to host memory ------------------------------------------
+    def _host_buffer(self, cam) -> torch.Tensor:
+        free = self._pinned[(cam.height, cam.width)]
+        if free:
+            return free.pop()
+        return torch.empty((cam.height, cam.width, 3), dtype=torch.uint8, pin_memory=True)
+
+    def release(self, req) -> None:
+        """Return a delivered request's host buffer to the pool."""
+        h = getattr(req, "host", None)
+        if h is not None:
+            self._pinned[(h.shape[0], h.shape[1])].append(h)
+            req.host = None
+
+    # -- lanes ----------------------------------------------------------------------
+    def _launch_large(self, slot: _LargeSlot, req) -> None:
+        s = self.scenes[req.scene]
+        cam = req.cam
+        with torch.cuda.stream(slot.stream):  # the caching allocator tracks the stream that writes it
+            out = torch.empty((cam.height, cam.width, 3), dtype=torch.uint8, device=self.device)
+        req.out = out
+        L = lib()
+        cp = (ctypes.c_float * 3)(*cam.position.reshape(-1).tolist())
+        cr = (ctypes.c_float * 9)(*cam.rotation.reshape(-1).tolist())
+        bgc = (ctypes.c_float * 3)(*self.bg)
+        st = L.gsr_forward_depth_first(
+            self.cfg.variant, s.num_vertex, s.position.data_ptr(), s.shs_half.data_ptr(), 1, s.opacity.data_ptr(),
+            s.cov3d.data_ptr(), cam.width, cam.height, self.cfg.block_x, self.cfg.block_y, cp, cr, cam.focal_x,
+            cam.focal_y, cam.zFar, cam.zNear, slot.counter.data_ptr(), slot.ws.data_ptr(), slot.ws.numel(),
+            slot.scratch.data_ptr(), slot.scratch.numel(), slot.tiles_u.data_ptr(), slot.vals_u.data_ptr(),
+            slot.tiles_s.data_ptr(), slot.vals_s.data_ptr(), slot.cap, slot.xy.data_ptr(), slot.rgbd.data_ptr(),
+            slot.con.data_ptr(), slot.ranges.data_ptr(), bgc, out.data_ptr(), ctypes.c_void_p(slot.stream.cuda_stream))
+        if st != R.GSR_OK:
+            raise GsrError(st, "forward_depth_first")
+        with torch.cuda.stream(slot.stream):
+            if self.deliver:
+                req.host = self._host_buffer(cam)
+                req.host.copy_(out, non_blocking=True)
+            slot.host[0:1].copy_(slot.counter, non_blocking=True)
+            slot.host[1:2].copy_(slot.ws[:4].view(torch.int32), non_blocking=True)
+            slot.event.record(slot.stream)
+        slot.job = req
+
+    def _launch_small(self, slot, reqs) -> None:
+        views = []
+        with torch.cuda.stream(self.s_small):  # the caching allocator tracks the lane that writes it
+            for r in reqs:
+                r.out = torch.empty((r.cam.height, r.cam.width, 3), dtype=torch.uint8, device=self.device)
+                views.append(View(r.scene, r.cam, self.bg, r.out))
+        b = slot["b"]
+        b.render(self.scenes, views, variant=self.cfg.variant, half=True, block_x=self.cfg.block_x,
+                 block_y=self.cfg.block_y, use_graph=True, stream=self.s_small)
+        with torch.cuda.stream(self.s_small):
+            if self.deliver:
+                for r in reqs:
+                    r.host = self._host_buffer(r.cam)
+                    r.host.copy_(r.out, non_blocking=True)
+            slot["host"].copy_(slot["ctr"], non_blocking=True)
+            slot["event"].record(self.s_small)
+        slot["job"] = list(reqs)
+
+    def _take_small(self, waiting) -> List:
+        """Requests for the next small batch: in arrival order, while the
+        batch's views, Gaussians, tiles and estimated keys fit."""
+        cfg = self.cfg
+        out, keys, g, tiles = [], 0, 0, 0
+        for r in list(waiting):
+            if len(out) >= cfg.max_views:
+                break
+            e = int(r.est * 1.25)
+            t = ((r.cam.width + cfg.block_x - 1) // cfg.block_x) * ((r.cam.height + cfg.block_y - 1) // cfg.block_y)
+            P = self.scenes[r.scene].num_vertex
+            if out and (keys + e > self.small_cap or g + P > self.max_g or tiles + t > self.tiles_cap):
+                break
+            out.append(r)
+            keys, g, tiles = keys + e, g + P, tiles + t
+        for r in out:
+            waiting.remove(r)
+        return out
+
+    # -- run ------------------------------------------------------------------------
+    def run(self, reqs, realtime: bool = True, deliver: bool = False):
+        """Serve `reqs` (objects with arrival_s, scene, camera).  Returns the
+        run's statistics; each request object gets `.out` (its image on the
+        device), `.latency_s` and, with `deliver`, `.host` (a pinned host copy
+        of the image, part of the request's latency; give it back with
+        `release`)."""
+        self.deliver = deliver
+        for r in reqs:
+            r.cam = Camera.from_spec(r.camera)
+            r.out = None
+        n = len(reqs)
+        waiting_small: collections.deque = collections.deque()
+        waiting_large: collections.deque = collections.deque()
+        done = 0
+        nxt = 0
+        batches, batched, large_n, retries = 0, 0, 0, 0
+        t0 = time.perf_counter()
+        base = reqs[0].arrival_s if (realtime and reqs) else 0.0
+        while done < n:
+            now = time.perf_counter() - t0
+            while nxt < n and (not realtime or reqs[nxt].arrival_s - base <= now):
+                r = reqs[nxt]
+                r.t_arrive = (r.arrival_s - base) if realtime else 0.0
+                r.est = self.est(r.scene, r.cam)
+                big = r.est >= self.cfg.large_keys or r.est * 1.25 > self.small_cap
+                (waiting_large if big else waiting_small).append(r)
+                nxt += 1
+            progressed = False
+            # retire finished work
+            for slot in self.large:
+                if slot.job is not None and slot.event.query():
+                    r, slot.job = slot.job, None
+                    keys, status = int(slot.host[0]), int(slot.host[1])
+                    if keys > slot.cap or status:
+                        # the large lane's buffers hold the largest frame the
+                        # budget allows: a frame beyond them is an error
+                        raise GsrError(R.GSR_TIMEOUT if status and keys <= slot.cap else R.GSR_OVERFLOW,
+                                       "serving (large lane)", keys)
+                    else:
+                        self.est.observe(r.scene, r.cam, keys)
+                        r.latency_s = time.perf_counter() - t0 - r.t_arrive
+                        done += 1
+                    progressed = True
+            for slot in self.small:
+                if slot["job"] is not None and slot["event"].query():
+                    job, slot["job"] = slot["job"], None
+                    keys = int(slot["host"][0])
+                    if keys > self.small_cap:
+                        # overflow: the counter still holds the batch's true key
+                        # count; learn from it and queue the requests again
+                        retries += 1
+                        self.est.observe_batch([(r.scene, r.cam) for r in job], keys)
+                        for r in reversed(job):
+                            r.est = max(self.est(r.scene, r.cam), int(keys / len(job)))
+                            (waiting_large if r.est >= self.cfg.large_keys or r.est > self.small_cap
+                             else waiting_small).appendleft(r)
+                    else:
+                        self.est.observe_batch([(r.scene, r.cam) for r in job], keys)
+                        tdone = time.perf_counter() - t0
+                        for r in job:
+                            r.latency_s = tdone - r.t_arrive
+                        done += len(job)
+                    progressed = True
+            # launch
+            for slot in self.large:
+                if slot.job is None and waiting_large:
+                    r = waiting_large.popleft()
+                    self._launch_large(slot, r)
+                    large_n += 1
+                    progressed = True
+            for slot in self.small:
+                if slot["job"] is None and waiting_small:
+                    job = self._take_small(waiting_small)
+                    self._launch_small(slot, job)
+                    batches += 1
+                    batched += len(job)
+                    progressed = True
+            if not progressed:
+                time.sleep(20e-6)
+        wall = time.perf_counter() - t0
+        st = _stats([r.latency_s for r in reqs], [r.camera.width for r in reqs], wall, batches=batches,
+                    mean_batch=batched / max(1, batches), large=large_n, retries=retries)
+        return st
+
+    def close(self):
+        torch.cuda.synchronize(self.device)
+        for s in self.small:
+            s["b"].close()
+        self.small = []
+        self.large = []
+
+
+# ----------------------------------------------------------------------------- autotuner
+DEFAULT_AXES = [(("block_x", "block_y"), [(32, 16), (32, 32)]),
+                ("large_keys", [2_000_000, 4_000_000, 16_000_000, 1 << 40]),
+                ("max_views", [4, 16]),
+                (("massive_area", "huge_area"), [(64, 4096), (16, 1024)])]
+
+
+def autotune(scenes, sample_reqs, device, budget_bytes: int = 60 << 30, log=None, axes=None,
+             start: Optional[TuneConfig] = None) -> Tuple[TuneConfig, list]:
+    """Coordinate search over the server's knobs, timing each candidate on
+    the same sample of requests served back to back (saturated).  Returns
+    the best configuration and the table of (config, frames/s)."""
+    table = []
+
+    def score(cfg: TuneConfig) -> float:
+        srv = Server(scenes, device, budget_bytes, cfg)
+        try:
+            srv.run(sample_reqs[: max(8, len(sample_reqs) // 4)], realtime=False)  # warm-up, graph capture
+            st = srv.run(sample_reqs, realtime=False)
+        finally:
+            srv.close()
+        table.append((dataclasses.asdict(cfg), st.frames_per_s))
+        if log:
+            log("autotune %s -> %.1f frames/s" % (dataclasses.asdict(cfg), st.frames_per_s))
+        return st.frames_per_s
+
+    best = start or TuneConfig()
+    best_fps = score(best)
+    axes = DEFAULT_AXES if axes is None else axes
+    tried = {tuple(sorted(dataclasses.asdict(best).items()))}
+    # two rounds of coordinate search: a knob's best value can move once
+    # another knob has changed (the tile shape moves the lane threshold)
+    for key, values in list(axes) + list(axes):
+        for v in values:
+            cand = dataclasses.replace(best)
+            if isinstance(key, tuple):
+                for k, x in zip(key, v):
+                    setattr(cand, k, x)
+            else:
+                setattr(cand, key, v)
+            sig = tuple(sorted(dataclasses.asdict(cand).items()))
+            if sig in tried:
+                continue
+            tried.add(sig)
+            f = score(cand)
+            if f > best_fps:
+                best, best_fps = cand, f
+    return best, table
