@@ -221,6 +221,7 @@ class Server:
             self.small.append({"b": b, "ctr": ctr, "host": torch.zeros(1, dtype=torch.int32, pin_memory=True),
                                "event": torch.cuda.Event(), "job": None})
         self.s_small = torch.cuda.Stream(self.device)
+        self.s_copy = torch.cuda.Stream(self.device)
         self.max_g = max_g
         self.tiles_cap = cfg.max_views * tiles_4k
         self.deliver = False
@@ -261,13 +262,30 @@ class Server:
         if st != R.GSR_OK:
             raise GsrError(st, "forward_depth_first")
         with torch.cuda.stream(slot.stream):
-            if self.deliver:
-                req.host = self._host_buffer(cam)
-                req.host.copy_(out, non_blocking=True)
             slot.host[0:1].copy_(slot.counter, non_blocking=True)
             slot.host[1:2].copy_(slot.ws[:4].view(torch.int32), non_blocking=True)
             slot.event.record(slot.stream)
+        self._deliver([req], slot.event)
         slot.job = req
+
+    def _deliver(self, reqs, computed: torch.cuda.Event) -> None:
+        """Copy the images of finished work to pinned host memory on the copy
+        stream, so the copies overlap the next kernels of the lanes."""
+        if not self.deliver:
+            for r in reqs:
+                r.delivered = None
+            return
+        self.s_copy.wait_event(computed)
+        ev = torch.cuda.Event()
+        with torch.cuda.stream(self.s_copy):
+            for r in reqs:
+                r.out.record_stream(self.s_copy)
+                self.release(r)  # a retried request's earlier copy lands first (same stream)
+                r.host = self._host_buffer(r.cam)
+                r.host.copy_(r.out, non_blocking=True)
+            ev.record(self.s_copy)
+        for r in reqs:
+            r.delivered = ev
 
     def _launch_small(self, slot, reqs) -> None:
         views = []
@@ -279,12 +297,9 @@ class Server:
         b.render(self.scenes, views, variant=self.cfg.variant, half=True, block_x=self.cfg.block_x,
                  block_y=self.cfg.block_y, use_graph=True, stream=self.s_small)
         with torch.cuda.stream(self.s_small):
-            if self.deliver:
-                for r in reqs:
-                    r.host = self._host_buffer(r.cam)
-                    r.host.copy_(r.out, non_blocking=True)
             slot["host"].copy_(slot["ctr"], non_blocking=True)
             slot["event"].record(self.s_small)
+        self._deliver(reqs, slot["event"])
         slot["job"] = list(reqs)
 
     def _take_small(self, waiting) -> List:
@@ -320,6 +335,7 @@ class Server:
         n = len(reqs)
         waiting_small: collections.deque = collections.deque()
         waiting_large: collections.deque = collections.deque()
+        delivering: collections.deque = collections.deque()  # computed, image copy in flight
         done = 0
         nxt = 0
         batches, batched, large_n, retries = 0, 0, 0, 0
@@ -347,8 +363,7 @@ class Server:
                                        "serving (large lane)", keys)
                     else:
                         self.est.observe(r.scene, r.cam, keys)
-                        r.latency_s = time.perf_counter() - t0 - r.t_arrive
-                        done += 1
+                        delivering.append(r)
                     progressed = True
             for slot in self.small:
                 if slot["job"] is not None and slot["event"].query():
@@ -365,11 +380,14 @@ class Server:
                              else waiting_small).appendleft(r)
                     else:
                         self.est.observe_batch([(r.scene, r.cam) for r in job], keys)
-                        tdone = time.perf_counter() - t0
-                        for r in job:
-                            r.latency_s = tdone - r.t_arrive
-                        done += len(job)
+                        delivering.extend(job)
                     progressed = True
+            # requests are complete once their image is where the client reads it
+            for r in [r for r in delivering if r.delivered is None or r.delivered.query()]:
+                delivering.remove(r)
+                r.latency_s = time.perf_counter() - t0 - r.t_arrive
+                done += 1
+                progressed = True
             # launch
             for slot in self.large:
                 if slot.job is None and waiting_large:
