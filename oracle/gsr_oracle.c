@@ -555,3 +555,204 @@ void ora_render(int64_t n, const uint32_t* vals, const int32_t* ranges, const fl
     render_worker(&jobs[0]);
     for (int i = 1; i < nthreads; i++) pthread_join(th[i], NULL);
 }
+
+/* ------------------------------------------------------------------------- */
+/* Differentiable-render reference (test infrastructure): the float image of
+ * one camera computed in double end to end from the raw parameters (means,
+ * log-scales, w-first quaternions, opacity logits, SH), with the tile
+ * emission, (tile, depth) order and whole-tile saturation exit of the
+ * forward (the same rules as ora_preprocess / ora_render, every continuous
+ * quantity in double).  The L2 loss against `target` is returned, so central
+ * differences of it check the gradients of the CUDA backward.  Tiles are
+ * rendered by nthreads threads; the result does not depend on the count. */
+typedef struct {
+    double px, py, depth, con[3], log2o, rgb[3];
+    int ok;
+} ora_dg;
+
+typedef struct {
+    uint32_t tile;
+    double depth;
+    uint32_t gid;
+} ora_pair;
+
+static int pair_cmp(const void* a, const void* b)
+{
+    const ora_pair* x = (const ora_pair*)a;
+    const ora_pair* y = (const ora_pair*)b;
+    if (x->tile != y->tile) return x->tile < y->tile ? -1 : 1;
+    if (x->depth != y->depth) return x->depth < y->depth ? -1 : 1;
+    return x->gid < y->gid ? -1 : (x->gid > y->gid);
+}
+
+typedef struct {
+    const ora_dg* g;
+    const ora_pair* pairs;
+    const int64_t* start;
+    int W, H, gx, tiles, cadence, tid, nthreads;
+    const double* bg;
+    double* img;
+} ora_dimg_job;
+
+static void* dimg_worker(void* arg)
+{
+    ora_dimg_job* j = (ora_dimg_job*)arg;
+    double T[256], C[256][3];
+    for (int t = j->tid; t < j->tiles; t += j->nthreads) {
+        int ox = (t % j->gx) * 16, oy = (t / j->gx) * 16;
+        for (int p = 0; p < 256; p++) { T[p] = 1.0; C[p][0] = C[p][1] = C[p][2] = 0.0; }
+        int64_t s = j->start[t], e = j->start[t + 1], processed = 0;
+        for (int64_t k = s; k < e; k++) {
+            const ora_dg* g = &j->g[j->pairs[k].gid];
+            for (int p = 0; p < 256; p++) {
+                double dx = g->px - (double)(ox + p % 16), dy = g->py - (double)(oy + p / 16);
+                double power = g->log2o + (-0.5 * ORA_LOG2E * g->con[0]) * dx * dx +
+                               (-0.5 * ORA_LOG2E * g->con[2]) * dy * dy + (-ORA_LOG2E * g->con[1]) * dx * dy;
+                double w = exp2(power) * T[p];
+                for (int ch = 0; ch < 3; ch++) C[p][ch] += g->rgb[ch] * w;
+                T[p] -= w;
+            }
+            processed++;
+            if (processed % j->cadence == 0) {
+                int sat = 1;
+                for (int p = 0; p < 256 && sat; p++) sat = T[p] < 0.0001;
+                if (sat) break;
+            }
+        }
+        for (int p = 0; p < 256; p++) {
+            int px = ox + p % 16, py = oy + p / 16;
+            if (px >= j->W || py >= j->H) continue;
+            double* o = j->img + 3 * ((size_t)py * j->W + px);
+            double tt = (e - s > 0) ? (T[p] < 0.0001 ? 0.0 : T[p]) : 1.0;
+            for (int ch = 0; ch < 3; ch++) o[ch] = (e - s > 0 ? C[p][ch] : 0.0) + tt * j->bg[ch];
+        }
+    }
+    return NULL;
+}
+
+double ora_image_fp64(int P, const double* means, const double* log_scales, const double* quats,
+                      const double* logits, const double* shs, int W, int H, const float* cam_pos,
+                      const float* cam_rot, double fx, double fy, const double* bg, int cadence,
+                      const double* target, double* img, int nthreads)
+{
+    ora_cam c;
+    make_cam(&c, W, H, cam_pos, cam_rot, fx, fy, 100.0, 0.01);
+    const int gx = (W + 15) / 16, gy = (H + 15) / 16, tiles = gx * gy;
+    const double tanx = W / (2.0 * fx), tany = H / (2.0 * fy);
+    ora_dg* g = (ora_dg*)calloc((size_t)(P > 0 ? P : 1), sizeof(ora_dg));
+    int64_t cap = 1024, n = 0;
+    ora_pair* pairs = (ora_pair*)malloc(sizeof(ora_pair) * cap);
+    for (int i = 0; i < P; i++) {
+        /* scene transform in double */
+        double o = 1.0 / (1.0 + exp(-logits[i]));
+        double s[3], q[4], qn = 0.0;
+        for (int k = 0; k < 3; k++) s[k] = exp(log_scales[3 * i + k]);
+        for (int k = 0; k < 4; k++) { q[k] = quats[4 * i + k]; qn += q[k] * q[k]; }
+        qn = sqrt(qn);
+        double r = q[0] / qn, x = q[1] / qn, y = q[2] / qn, z = q[3] / qn;
+        double R[3][3] = {{1 - 2 * (y * y + z * z), 2 * (x * y - r * z), 2 * (x * z + r * y)},
+                          {2 * (x * y + r * z), 1 - 2 * (x * x + z * z), 2 * (y * z - r * x)},
+                          {2 * (x * z - r * y), 2 * (y * z + r * x), 1 - 2 * (x * x + y * y)}};
+        double Sg[3][3];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                double acc = 0.0;
+                for (int k = 0; k < 3; k++) acc += R[a][k] * s[k] * s[k] * R[b][k];
+                Sg[a][b] = acc;
+            }
+        const double* m = means + 3 * i;
+        double t[3], hom[4];
+        for (int rr = 0; rr < 3; rr++)
+            t[rr] = c.view[rr][0] * m[0] + c.view[rr][1] * m[1] + c.view[rr][2] * m[2] + c.view[rr][3];
+        if (t[2] <= 0.2) continue;
+        for (int rr = 0; rr < 4; rr++)
+            hom[rr] = c.proj[rr][0] * m[0] + c.proj[rr][1] * m[1] + c.proj[rr][2] * m[2] + c.proj[rr][3];
+        double pw = 1.0 / (hom[3] + 0.0000001);
+        double limx = 1.3 * tanx, limy = 1.3 * tany;
+        double tz = t[2];
+        double tx = fmin(limx, fmax(-limx, t[0] / tz)) * tz, ty = fmin(limy, fmax(-limy, t[1] / tz)) * tz;
+        double J[2][3] = {{fx / tz, 0.0, -(fx * tx) / (tz * tz)}, {0.0, fy / tz, -(fy * ty) / (tz * tz)}};
+        double Tm[2][3];
+        for (int a = 0; a < 2; a++)
+            for (int k = 0; k < 3; k++)
+                Tm[a][k] = J[a][0] * c.view[0][k] + J[a][1] * c.view[1][k] + J[a][2] * c.view[2][k];
+        double cv[2][2];
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++) {
+                double acc = 0.0;
+                for (int k = 0; k < 3; k++)
+                    for (int l = 0; l < 3; l++) acc += Tm[a][k] * Sg[k][l] * Tm[b][l];
+                cv[a][b] = acc;
+            }
+        double cxx = cv[0][0] + 0.3, cxy = cv[0][1], cyy = cv[1][1] + 0.3;
+        double det = cxx * cyy - cxy * cxy;
+        ora_dg* G = &g[i];
+        G->con[0] = cyy / det;
+        G->con[1] = -cxy / det;
+        G->con[2] = cxx / det;
+        G->log2o = log2(o);
+        double power = ORA_LN2 * 8.0 + ORA_LN2 * G->log2o;
+        if (2.0 * det * power < 0.09 * (cxx + cyy) && o < 0.5) continue;
+        int w = (int)(1.414214 * sqrt(cxx * power) + 1.0), h = (int)(1.414214 * sqrt(cyy * power) + 1.0);
+        G->px = ((hom[0] * pw + 1.0) * W - 1.0) * 0.5;
+        G->py = ((hom[1] * pw + 1.0) * H - 1.0) * 0.5;
+        G->depth = tz;
+        double dir[3] = {m[0] - c.campos[0], m[1] - c.campos[1], m[2] - c.campos[2]};
+        double l = sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+        double X = dir[0] / l, Y = dir[1] / l, Z = dir[2] / l;
+        double xx = X * X, yy = Y * Y, zz = Z * Z;
+        double B[16] = {C0, -C1 * Y, C1 * Z, -C1 * X, C2[0] * X * Y, C2[1] * Y * Z, C2[2] * (2 * zz - xx - yy),
+                        C2[3] * X * Z, C2[4] * (xx - yy), C3[0] * Y * (3 * xx - yy), C3[1] * X * Y * Z,
+                        C3[2] * Y * (4 * zz - xx - yy), C3[3] * Z * (2 * zz - 3 * xx - 3 * yy),
+                        C3[4] * X * (4 * zz - xx - yy), C3[5] * Z * (xx - yy), C3[6] * X * (xx - 3 * yy)};
+        for (int ch = 0; ch < 3; ch++) {
+            double acc = 0.5;
+            for (int k = 0; k < 16; k++) acc += B[k] * shs[48 * (size_t)i + 3 * k + ch];
+            G->rgb[ch] = acc > 0.0 ? acc : 0.0;
+        }
+        /* rectangle and tile test as the forward (centre rounded to float) */
+        ora_geom tg;
+        memset(&tg, 0, sizeof tg);
+        tg.px = G->px; tg.py = G->py; tg.power = power;
+        tg.con[0] = G->con[0]; tg.con[1] = G->con[1]; tg.con[2] = G->con[2];
+        double fpx = (float)G->px, fpy = (float)G->py;
+        int x0 = imin(gx, imax(0, (int)((fpx - w) / 16))), y0 = imin(gy, imax(0, (int)((fpy - h) / 16)));
+        int x1 = imin(gx, imax(0, (int)((fpx + w) / 16) + 1)), y1 = imin(gy, imax(0, (int)((fpy + h) / 16) + 1));
+        for (int yy2 = y0; yy2 < y1; yy2++)
+            for (int xx2 = x0; xx2 < x1; xx2++) {
+                if (!tile_hit(&tg, xx2, yy2, 16, 16)) continue;
+                if (n == cap) { cap *= 2; pairs = (ora_pair*)realloc(pairs, sizeof(ora_pair) * cap); }
+                pairs[n].tile = (uint32_t)(yy2 * gx + xx2);
+                pairs[n].depth = tz;
+                pairs[n].gid = (uint32_t)i;
+                n++;
+            }
+        G->ok = 1;
+    }
+    qsort(pairs, (size_t)n, sizeof(ora_pair), pair_cmp);
+    int64_t* start = (int64_t*)calloc((size_t)tiles + 1, sizeof(int64_t));
+    for (int64_t k = 0; k < n; k++) start[pairs[k].tile + 1]++;
+    for (int t = 0; t < tiles; t++) start[t + 1] += start[t];
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    ora_dimg_job jobs[256];
+    for (int i = 0; i < nthreads; i++) {
+        ora_dimg_job* jb = &jobs[i];
+        jb->g = g; jb->pairs = pairs; jb->start = start; jb->W = W; jb->H = H; jb->gx = gx; jb->tiles = tiles;
+        jb->cadence = cadence > 0 ? cadence : 1; jb->tid = i; jb->nthreads = nthreads; jb->bg = bg; jb->img = img;
+    }
+    for (int i = 1; i < nthreads; i++) pthread_create(&th[i], NULL, dimg_worker, &jobs[i]);
+    dimg_worker(&jobs[0]);
+    for (int i = 1; i < nthreads; i++) pthread_join(th[i], NULL);
+    double loss = 0.0;
+    if (target)
+        for (size_t k = 0; k < (size_t)W * H * 3; k++) {
+            double d = img[k] - target[k];
+            loss += d * d;
+        }
+    free(start);
+    free(pairs);
+    free(g);
+    return loss;
+}

@@ -59,6 +59,9 @@ def lib():
         L.ora_gather.restype = None
         L.ora_render.argtypes = [i64, P, P, P, P, P, i32, i32, i32, i32, i32, i32, P, P, P, i32]
         L.ora_render.restype = None
+        L.ora_image_fp64.argtypes = [i32, P, P, P, P, P, i32, i32, P, P, ctypes.c_double, ctypes.c_double, P, i32, P,
+                                     P, i32]
+        L.ora_image_fp64.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -185,3 +188,22 @@ def forward(pos, shs, opacity, cov3d, cam, bg=(0.0, 0.0, 0.0), bx=16, by=16, cad
                  cadence, nthreads=nthreads)
     pre.update(keys_sorted=ks, vals_sorted=vs, ranges=rng, end_bit=eb)
     return img, pre
+
+
+def image_fp64(means, log_scales, quats, logits, shs, cam, bg=(0.0, 0.0, 0.0), cadence=8, target=None,
+               nthreads=None):
+    """The float image of one camera in double end to end from raw parameters
+    (gsr_oracle.c ora_image_fp64) and, with `target`, its L2 loss.
+    Returns (loss, image [H,W,3] float64)."""
+    f8 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    m, ls, q, lg, sh = f8(means), f8(log_scales), f8(quats), f8(logits), f8(shs).reshape(-1, 48)
+    P = lg.shape[0]
+    img = np.zeros((cam.height, cam.width, 3), np.float64)
+    cp, cr = _c(cam.position, np.float32).reshape(3), _c(cam.rotation, np.float32).reshape(9)
+    b = f8(bg).reshape(3)
+    tgt = f8(target) if target is not None else None
+    loss = lib().ora_image_fp64(P, _p(m), _p(ls), _p(q), _p(lg), _p(sh), cam.width, cam.height, _p(cp), _p(cr),
+                                float(cam.fx), float(cam.fy), _p(b), int(cadence),
+                                _p(tgt) if tgt is not None else None, _p(img), nthreads or nthreads_default())
+    return float(loss), img
+

@@ -217,6 +217,30 @@ struct RenderArgs {
 };
 cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream);
 
+// Differentiable render (16x16 tiles, lite exit cadence 8): the forward
+// writes `image` (float [H,W,3]), `T_final` ([H,W]) and `n_tile` ([tiles]);
+// the backward reads them with `grad_image` and accumulates the per-Gaussian
+// gradients of xy [P,2], conic/opacity [P,4] and colour [P,3].
+struct TrainRenderArgs {
+    int W, H, P;
+    const int32_t* d_num;
+    long long cap;
+    const uint32_t* vals;
+    const int2* ranges;
+    const float2* xy;
+    const float4* rgbd;
+    const float4* con;
+    float bg[3];
+    float* image;
+    float* T_final;
+    int32_t* n_tile;
+    const float* grad_image;
+    float* grad_xy;
+    float* grad_con;
+    float* grad_rgb;
+};
+cudaError_t launch_render_train(const TrainRenderArgs& a, bool backward, cudaStream_t stream);
+
 // One view of a batched render: its tiles are [tile_base, tile_base +
 // gx * gy) of the batch's global tile ids.
 struct RenderView {

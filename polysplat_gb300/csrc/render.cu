@@ -430,6 +430,237 @@ cudaError_t dispatch_batch(int variant, const RenderParams& p, cudaStream_t stre
 
 static cudaError_t launch_prepared(const RenderArgs& a, RenderParams& p, cudaStream_t stream);
 
+// ---------------------------------------------------------------------------
+// Differentiable render (no counterpart in the reference): the forward of the
+// persistent lite render (16x16 tiles, exit check every 8 Gaussians, same
+// per-pixel arithmetic through shade<>) writing a float image, each pixel's
+// final transmittance and each tile's number of blended Gaussians; and its
+// backward, which walks every tile's list in reverse.
+
+namespace {
+
+constexpr int kTrainWarps = 4;
+constexpr int kTrainCadence = 8;
+
+struct TrainBatch {
+    float2 xy[32];
+    float4 con[32];
+    float4 rgb[32];
+    uint32_t gid[32];
+};
+
+__global__ __launch_bounds__(kTrainWarps * 32) void k_render_train(const TrainRenderArgs a)
+{
+    __shared__ TrainBatch sb[kTrainWarps];
+    const unsigned lane = threadIdx.x & 31u;
+    const int warp = threadIdx.x >> 5;
+    TrainBatch& B = sb[warp];
+    const int gx = (a.W + 15) / 16, tiles = gx * ((a.H + 15) / 16);
+    const int tile = blockIdx.x * kTrainWarps + warp;
+    if (tile >= tiles) return;
+    const int n = (int)max(0LL, min((long long)*a.d_num, a.cap));
+    const int ox = (tile % gx) * 16, oy = (tile / gx) * 16;
+    const int cb = (int)(lane & 7u) * 2, rb = (int)(lane >> 3) * 4;
+    const int2 rg = __ldg(a.ranges + tile);
+    const int start = min(max(rg.x, 0), n), end = min(max(rg.y, start), n);
+    float T[4][2], C[4][2][3];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            T[i][j] = 1.0f;
+            C[i][j][0] = C[i][j][1] = C[i][j][2] = 0.0f;
+        }
+    int processed = 0;
+    bool exit_now = false;
+    for (int pos = start; pos < end && !exit_now; pos += 32) {
+        const int cnt = min(32, end - pos);
+        __syncwarp();
+        if ((int)lane < cnt) {
+            const uint32_t g = __ldg(a.vals + pos + lane);
+            if (g < (uint32_t)a.P) {
+                B.xy[lane] = __ldg(a.xy + g);
+                B.con[lane] = __ldg(a.con + g);
+                B.rgb[lane] = __ldg(a.rgbd + g);
+            } else {  // outside the feature arrays: a transparent stand-in
+                B.xy[lane] = make_float2(0.f, 0.f);
+                B.con[lane] = make_float4(0.f, 0.f, 0.f, -1e30f);
+                B.rgb[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+        __syncwarp();
+        for (int k = 0; k < cnt; k++) {
+            const float4 rgb = B.rgb[k];
+            shade<2, 4, 0, false>(C, T, ox, oy, cb, rb, B.xy[k], B.con[k], make_float3(rgb.x, rgb.y, rgb.z));
+            ++processed;
+            if (processed % kTrainCadence == 0) {
+                bool sat = true;
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int j = 0; j < 2; j++) sat = sat && T[i][j] < 0.0001f;
+                if (__all_sync(GSR_FULL_MASK, sat)) {
+                    exit_now = true;
+                    break;
+                }
+            }
+        }
+    }
+    if (lane == 0) a.n_tile[tile] = processed;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int px = ox + cb + j, py = oy + rb + i;
+            if (px >= a.W || py >= a.H) continue;
+            const size_t o = (size_t)py * a.W + px;
+            const float t = T[i][j], tt = t < 0.0001f ? 0.0f : t;
+            a.T_final[o] = t;
+            a.image[3 * o + 0] = C[i][j][0] + tt * a.bg[0];
+            a.image[3 * o + 1] = C[i][j][1] + tt * a.bg[1];
+            a.image[3 * o + 2] = C[i][j][2] + tt * a.bg[2];
+        }
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(GSR_FULL_MASK, v, d);
+    return v;
+}
+
+// Reverse traversal of each tile's blended Gaussians.  With T_after the
+// transmittance behind Gaussian i and alpha_i recomputed bit for bit,
+// T_before = T_after / (1 - alpha_i) (1 - alpha is exact once alpha >= 1/2);
+// R, the colour composited behind i per unit transmittance, starts at bg (or
+// 0 where the forward dropped the background term) and follows
+// R <- alpha c + (1 - alpha) R.  Then
+//   dL/dc_i     = sum_px alpha_i T_before dL/dC
+//   dL/dalpha_i = T_before (c_i - R) . dL/dC,   d alpha/d power = alpha ln 2
+// and the power's derivatives give the conic/opacity and centre gradients.
+// The 9 per-Gaussian sums are reduced over the warp and added atomically.
+__global__ __launch_bounds__(kTrainWarps * 32) void k_render_backward(const TrainRenderArgs a)
+{
+    __shared__ TrainBatch sb[kTrainWarps];
+    const unsigned lane = threadIdx.x & 31u;
+    const int warp = threadIdx.x >> 5;
+    TrainBatch& B = sb[warp];
+    const int gx = (a.W + 15) / 16, tiles = gx * ((a.H + 15) / 16);
+    const int tile = blockIdx.x * kTrainWarps + warp;
+    if (tile >= tiles) return;
+    const int n = (int)max(0LL, min((long long)*a.d_num, a.cap));
+    const int ox = (tile % gx) * 16, oy = (tile / gx) * 16;
+    const int cb = (int)(lane & 7u) * 2, rb = (int)(lane >> 3) * 4;
+    const int2 rg = __ldg(a.ranges + tile);
+    const int start = min(max(rg.x, 0), n);
+    const int count = min(max(__ldg(a.n_tile + tile), 0), max(0, min(max(rg.y, start), n) - start));
+    float T[4][2], R[4][2][3], G[4][2][3];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int px = ox + cb + j, py = oy + rb + i;
+            const bool in = px < a.W && py < a.H;
+            const size_t o = in ? (size_t)py * a.W + px : 0;
+            const float t = in ? __ldg(a.T_final + o) : 1.0f;
+            T[i][j] = t;
+#pragma unroll
+            for (int ch = 0; ch < 3; ch++) {
+                R[i][j][ch] = t < 0.0001f ? 0.0f : a.bg[ch];
+                G[i][j][ch] = in ? __ldg(a.grad_image + 3 * o + ch) : 0.0f;
+            }
+        }
+    const float LN2 = 0.69314718055994531f;
+    for (int hi = start + count; hi > start; hi -= 32) {
+        const int lo = max(start, hi - 32), cnt = hi - lo;
+        __syncwarp();
+        if ((int)lane < cnt) {
+            const uint32_t g = __ldg(a.vals + lo + lane);
+            const bool ok = g < (uint32_t)a.P;
+            B.gid[lane] = ok ? g : 0xFFFFFFFFu;
+            B.xy[lane] = ok ? __ldg(a.xy + g) : make_float2(0.f, 0.f);
+            B.con[lane] = ok ? __ldg(a.con + g) : make_float4(0.f, 0.f, 0.f, -1e30f);
+            B.rgb[lane] = ok ? __ldg(a.rgbd + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        __syncwarp();
+        for (int k = cnt - 1; k >= 0; k--) {
+            const float2 xy = B.xy[k];
+            const float4 co = B.con[k];
+            const float4 c4 = B.rgb[k];
+            const float col[3] = {c4.x, c4.y, c4.z};
+            float gcon[4] = {0.f, 0.f, 0.f, 0.f}, gxy[2] = {0.f, 0.f}, gc[3] = {0.f, 0.f, 0.f};
+            // the forward's per-pixel power, term for term (shade<>, SHADER 0)
+            float xs[2], xc[2], dxs[2];
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const float dx = xy.x - (float)(ox + cb + j);
+                dxs[j] = dx;
+                xs[j] = co.x * dx * dx;
+                xc[j] = co.y * dx;
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const float dy = xy.y - (float)(oy + rb + i);
+                const float ys = co.z * dy * dy;
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    const float power = fmaf(xc[j], dy, co.w + xs[j] + ys);
+                    const float alpha = ex2_approx_ftz(power);
+                    const float one_m = 1.0f - alpha;
+                    const float Tb = one_m > 0.0f ? fminf(1.0f, T[i][j] / one_m) : T[i][j];
+                    const float w = alpha * Tb;
+                    float dalpha = 0.0f;
+#pragma unroll
+                    for (int ch = 0; ch < 3; ch++) {
+                        gc[ch] += w * G[i][j][ch];
+                        dalpha += (col[ch] - R[i][j][ch]) * G[i][j][ch];
+                        R[i][j][ch] = alpha * col[ch] + one_m * R[i][j][ch];
+                    }
+                    T[i][j] = Tb;
+                    const float dp = dalpha * Tb * alpha * LN2;
+                    const float dx = dxs[j];
+                    gcon[3] += dp;
+                    gcon[0] += dp * dx * dx;
+                    gcon[2] += dp * dy * dy;
+                    gcon[1] += dp * dx * dy;
+                    gxy[0] += dp * (2.0f * co.x * dx + co.y * dy);
+                    gxy[1] += dp * (2.0f * co.z * dy + co.y * dx);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) gcon[q] = warp_sum(gcon[q]);
+#pragma unroll
+            for (int q = 0; q < 2; q++) gxy[q] = warp_sum(gxy[q]);
+#pragma unroll
+            for (int q = 0; q < 3; q++) gc[q] = warp_sum(gc[q]);
+            const uint32_t gid = B.gid[k];
+            if (lane == 0 && gid != 0xFFFFFFFFu) {
+                atomicAdd(a.grad_con + 4 * (size_t)gid + 0, gcon[0]);
+                atomicAdd(a.grad_con + 4 * (size_t)gid + 1, gcon[1]);
+                atomicAdd(a.grad_con + 4 * (size_t)gid + 2, gcon[2]);
+                atomicAdd(a.grad_con + 4 * (size_t)gid + 3, gcon[3]);
+                atomicAdd(a.grad_xy + 2 * (size_t)gid + 0, gxy[0]);
+                atomicAdd(a.grad_xy + 2 * (size_t)gid + 1, gxy[1]);
+                atomicAdd(a.grad_rgb + 3 * (size_t)gid + 0, gc[0]);
+                atomicAdd(a.grad_rgb + 3 * (size_t)gid + 1, gc[1]);
+                atomicAdd(a.grad_rgb + 3 * (size_t)gid + 2, gc[2]);
+            }
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_render_train(const TrainRenderArgs& a, bool backward, cudaStream_t stream)
+{
+    const int tiles = ((a.W + 15) / 16) * ((a.H + 15) / 16);
+    if (tiles <= 0) return cudaSuccess;
+    const int grid = div_up(tiles, kTrainWarps);
+    if (backward) k_render_backward<<<grid, kTrainWarps * 32, 0, stream>>>(a);
+    else k_render_train<<<grid, kTrainWarps * 32, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream)
 {
     RenderParams p;
