@@ -219,6 +219,8 @@ def run_gsr(args):
     dev = torch.device("cuda", local)
     if args.workload == "serve_mix":
         line = run_serve(args, dev, rank, world, dist)
+    elif args.workload == "diff_1m_8cam":
+        line = run_diff(args, dev, rank, world, dist)
     else:
         line = forward_line(args, dev, rank, world, dist)
     if rank == 0 and line is not None:
@@ -399,9 +401,21 @@ def forward_line(args, dev, rank, world, dist):
                 b.synchronize()
                 ts.append(a.elapsed_time(b))
             ref_ms = statistics.mean(ts)
-            ref_img_equal = bool(torch.equal(pipe.out, rast.forward(scene, cam, bg, render_variant=E2E_VARIANT)))
+            ref_first = pipe.out.clone()
+            pipe.forward()
+            torch.cuda.synchronize()
+            ds = (pipe.out.int() - ref_first.int()).abs()
+            ref_self = {"max_abs": int(ds.max()), "frac_diff": float((ds > 0).double().mean())}
+            mine = rast.forward(scene, cam, bg, render_variant=E2E_VARIANT)
+            ref_img_equal = bool(torch.equal(pipe.out, mine))
+            d = (pipe.out.int() - mine.int()).abs()
+            mse = float((d.double() ** 2).mean())
+            img_cmp = {"max_abs": int(d.max()), "frac_diff": float((d > 0).double().mean()),
+                       "psnr_db": (10.0 * np.log10(255.0 ** 2 / mse)) if mse > 0 else None}
             ref_gpu = {"value": 1000.0 / ref_ms, "unit": "frames/s", "ms_per_frame": ref_ms,
                        "median_ms": statistics.median(ts), "num_rendered": n_ref, "image_identical": ref_img_equal,
+                       "image_vs_this_library": img_cmp,
+                       "reference_run_vs_run": ref_self,
                        "what": "reference preprocess/render kernels built from its sources + its CUB SortPairs "
                                "call, E2E sequence of forward_fused_e2e incl. its per-frame count read-back"}
             del pipe
@@ -535,6 +549,70 @@ def run_serve(args, dev, rank, world, dist):
             if fwd else None,
             "cpu_baseline": cpu,
             "gpu_launches": launches, "clocks": clocks}
+
+
+def run_diff(args, dev, rank, world, dist):
+    """Config 4: 1 M Gaussians (means ~ N(0, 3^2 I)), 8 cameras at 1280x720 on
+    a radius-10 orbit, L2 loss against renders of perturbed means and SH DC.
+    A step is the forward of the 8 views, the loss and the backward to every
+    raw parameter; `value` is views per second."""
+    import numpy as np
+    import torch
+
+    from polysplat_gb300 import Camera, scenes
+    from polysplat_gb300.diff import render
+
+    raw, cams = scenes.workload("diff_1m_8cam")
+    rng = np.random.default_rng(4)
+    cams = [Camera.from_spec(c) for c in cams]
+    t = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float32, device=dev)
+    params = [t(raw.means), t(raw.log_scales), t(raw.quats), t(raw.opacity_logits), t(raw.shs.reshape(-1, 48))]
+    tm = t(raw.means + rng.normal(0, 0.05, raw.means.shape))
+    tsh = raw.shs.copy()
+    tsh[:, 0, :] += rng.normal(0, 0.1, tsh[:, 0, :].shape)
+    with torch.no_grad():
+        targets = [render(tm, params[1], params[2], params[3], t(tsh.reshape(-1, 48)), c) for c in cams]
+    for p in params:
+        p.requires_grad_(True)
+
+    def step():
+        for p in params:
+            p.grad = None
+        loss = sum(((render(*params, c) - tg) ** 2).sum() for c, tg in zip(cams, targets))
+        loss.backward()
+        return loss
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    K = max(3, min(args.steps, 30))
+    sampler = ClockSampler(dev.index or 0)
+    if dist is not None:
+        dist.barrier()
+    sampler.start()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(K):
+        step()
+    b.record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = a.elapsed_time(b) / K
+    if dist is not None:
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    if rank != 0:
+        return None
+    views = world * len(cams) * 1000.0 / ms
+    return {"metric": "views/s (forward + backward)", "value": views, "unit": "views/s", "n_gpus": world,
+            "steps": K, "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "diff_1m_8cam", "gaussians": raw.num, "views": len(cams),
+                       "resolution": "1280x720", "loss": "L2", "grads": "means, log-scales, quats, logits, SH",
+                       "l2": "scene 1 M Gaussians (0.3 GB fp32 parameters + per-view lists), larger than L2"},
+            "e2e": {"value": views, "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 4},
+            "gpu_launches": K * len(cams) * 15, "clocks": clocks}
 
 
 def serve_cpu_baseline(raws, reqs, seconds: float):

@@ -5,12 +5,14 @@
 // render.cu:1736-1737).  Warps take tiles from a per-launch atomic queue in
 // the caller's workspace (no module-global counter, so concurrent launches on
 // different workspaces are safe).  The Gaussians of a tile are consumed in
-// batches of 32: for each batch every lane issues 1-D TMA bulk copies
-// (cp.async.bulk) of its Gaussian's conic/opacity, colour/depth and centre
-// records into one half of a double-buffered shared-memory ring whose
-// completion is tracked by an mbarrier transaction count, so the next batch
-// streams in while the current one is blended.  Every wait is bounded: on
-// expiry the warp records a timeout in the status word and stops.
+// batches of 32: for each batch every lane copies its Gaussian's
+// conic/opacity, colour/depth and centre records into one half of a
+// double-buffered shared-memory ring with per-thread cp.async copies, so the
+// next batch streams in while the current one is blended.  A second staging
+// path issues 1-D TMA bulk copies (cp.async.bulk) completed on an mbarrier
+// (GSR_RENDER_TMA=1); for these 16-byte gathers it measured slower.  Every
+// wait is bounded: on expiry the warp records a timeout in the status word
+// and stops.
 //
 // The blend of each Gaussian-pixel pair is the reference's arithmetic
 // (pixel_shader_axis_shared_16x16 / pixel_shader, render.cu:228-271 and
@@ -18,6 +20,9 @@
 // skip, front-to-back compositing, and a whole-tile exit once every pixel of
 // the tile has T < 1e-4, checked every CADENCE Gaussians.  Output is the
 // truncating uint8 encode of render.cu:375-394.
+#include <cstdlib>
+#include <cstring>
+
 #include "gsr_internal.h"
 
 namespace gsr {
@@ -410,18 +415,18 @@ cudaError_t dispatch_shape(int variant, bool tma, const RenderParams& p, cudaStr
     }
 }
 
-// Batched renders: ranges always precomputed, TMA staging (the batch's own
-// feature buffers are aligned), 16x16, 32x16 and 32x32 tiles.
+// Batched renders: ranges always precomputed, cp.async staging, 16x16,
+// 32x16 and 32x32 tiles.
 template <int BX, int BY>
 cudaError_t dispatch_batch(int variant, const RenderParams& p, cudaStream_t stream)
 {
     constexpr int SH = (BX == 16 && BY == 16) ? 0 : 1;
     switch (variant) {
-    case GSR_RENDER_PERSISTENT_RANGES: return launch_variant<BX, BY, 8, 0, false, 0, true, true>(p, stream);
-    case GSR_RENDER_PERSISTENT_FUSED: return launch_variant<BX, BY, 16, 0, false, 0, true, true>(p, stream);
+    case GSR_RENDER_PERSISTENT_RANGES: return launch_variant<BX, BY, 8, 0, false, 0, false, true>(p, stream);
+    case GSR_RENDER_PERSISTENT_FUSED: return launch_variant<BX, BY, 16, 0, false, 0, false, true>(p, stream);
     case GSR_RENDER_DEFAULT:
-    case GSR_RENDER_RANGES_CADENCE2: return launch_variant<BX, BY, 2, SH, false, 0, true, true>(p, stream);
-    case GSR_RENDER_DT: return launch_variant<BX, BY, 8, 0, true, 0, true, true>(p, stream);
+    case GSR_RENDER_RANGES_CADENCE2: return launch_variant<BX, BY, 2, SH, false, 0, false, true>(p, stream);
+    case GSR_RENDER_DT: return launch_variant<BX, BY, 8, 0, true, 0, false, true>(p, stream);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -429,6 +434,19 @@ cudaError_t dispatch_batch(int variant, const RenderParams& p, cudaStream_t stre
 }  // namespace
 
 static cudaError_t launch_prepared(const RenderArgs& a, RenderParams& p, cudaStream_t stream);
+
+static bool use_render_tma()
+{
+    static int mode = -1;
+    if (mode < 0) {
+        // per-thread cp.async staging measured faster than per-lane 16-byte
+        // bulk copies (28 vs 48 us at 1080p, 2.5 vs 3.6 ms at 8K): bulk
+        // copies only on request
+        const char* e = getenv("GSR_RENDER_TMA");
+        mode = (e && strcmp(e, "1") == 0) ? 1 : 0;
+    }
+    return mode == 1;
+}
 
 // ---------------------------------------------------------------------------
 // Differentiable render (no counterpart in the reference): the forward of the
@@ -718,11 +736,14 @@ static cudaError_t launch_prepared(const RenderArgs& a, RenderParams& p, cudaStr
     if (p.tiles <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(p.queue, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
-    // TMA bulk copies need 16-byte aligned feature arrays.
-    const bool tma = ((reinterpret_cast<uintptr_t>(a.xy) | reinterpret_cast<uintptr_t>(a.rgbd) |
-                       reinterpret_cast<uintptr_t>(a.con)) & 15u) == 0;
+    // TMA bulk copies need 16-byte aligned feature arrays; GSR_RENDER_TMA=0
+    // stages batches with per-thread cp.async copies instead.
+    const bool tma = use_render_tma() && ((reinterpret_cast<uintptr_t>(a.xy) | reinterpret_cast<uintptr_t>(a.rgbd) |
+                                           reinterpret_cast<uintptr_t>(a.con)) & 15u) == 0;
     if (p.views) {
-        if (!tma || !p.ranges) return cudaErrorInvalidValue;
+        if (!p.ranges || ((reinterpret_cast<uintptr_t>(a.xy) | reinterpret_cast<uintptr_t>(a.rgbd) |
+                           reinterpret_cast<uintptr_t>(a.con)) & 15u) != 0)
+            return cudaErrorInvalidValue;
         if (a.bx == 16 && a.by == 16) return dispatch_batch<16, 16>(a.variant, p, stream);
         if (a.bx == 32 && a.by == 16) return dispatch_batch<32, 16>(a.variant, p, stream);
         if (a.bx == 32 && a.by == 32) return dispatch_batch<32, 32>(a.variant, p, stream);

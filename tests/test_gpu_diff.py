@@ -77,3 +77,48 @@ def test_gradients_match_fp64_finite_differences(cuda_device):
     good = np.abs(gg - fd) <= 0.05 * np.abs(fd) + 0.01 * scale
     print("\nagree %d/64; worst rel %s" % (good.sum(), np.sort(np.abs(gg - fd) / (np.abs(fd) + 1e-12))[-5:]))
     assert good.sum() >= 60, list(zip(picks, gg, fd))
+
+
+def test_gradients_config4_distribution(cuda_device):
+    """The config-4 distribution (means ~ N(0, 3^2 I), 8 cameras on a
+    radius-10 orbit), subsampled to 4000 Gaussians at 256x144 so the FP64
+    oracle evaluates the loss quickly; same bar as above."""
+    import math
+
+    full = scenes.scene_plain_small(1_000_000, seed=4, mean_sigma=3.0)
+    raw = scenes.subsample(full, 4000, seed=1)
+    cams = [scenes.orbit_camera(10.0, 2 * math.pi * k / 8, 0.0, 256, 144, 180.0) for k in range(8)]
+    rng = np.random.default_rng(4)
+    tmeans = raw.means + rng.normal(0, 0.05, raw.means.shape).astype(np.float32)
+    tshs = raw.shs.copy()
+    tshs[:, 0, :] += rng.normal(0, 0.1, tshs[:, 0, :].shape).astype(np.float32)
+    targets = [O.image_fp64(tmeans, raw.log_scales, raw.quats, raw.opacity_logits, tshs, c)[1] for c in cams]
+    dev = cuda_device
+    params = [torch.tensor(a, dtype=torch.float32, device=dev, requires_grad=True)
+              for a in (raw.means, raw.log_scales, raw.quats, raw.opacity_logits, raw.shs.reshape(-1, 48))]
+    loss = sum(((render(*params, Camera.from_spec(c)) - torch.tensor(t, dtype=torch.float32, device=dev)) ** 2).sum()
+               for c, t in zip(cams, targets))
+    loss.backward()
+    grads = [p.grad.detach().cpu().numpy().astype(np.float64) for p in params]
+    theta = [np.asarray(a, np.float64).copy() for a in (raw.means, raw.log_scales, raw.quats, raw.opacity_logits,
+                                                        raw.shs.reshape(-1, 48))]
+    rng = np.random.default_rng(12)
+    active = np.flatnonzero(np.abs(grads[0]).sum(1) > 1e-3 * np.abs(grads[0]).sum(1).max())
+    picks = [(int(rng.choice(5, p=[0.25, 0.2, 0.2, 0.15, 0.2])), int(rng.choice(active))) for _ in range(64)]
+    picks = [(t, g, int(rng.integers(0, theta[t].shape[1])) if theta[t].ndim == 2 else 0) for t, g in picks]
+    h = 1e-4
+    fd, gg = [], []
+    for t, g, k in picks:
+        idx = (g, k) if theta[t].ndim == 2 else (g,)
+        old = theta[t][idx]
+        theta[t][idx] = old + h
+        lp = _loss_fp64(theta, raw, cams, targets)
+        theta[t][idx] = old - h
+        lm = _loss_fp64(theta, raw, cams, targets)
+        theta[t][idx] = old
+        fd.append((lp - lm) / (2 * h))
+        gg.append(grads[t][idx])
+    fd, gg = np.array(fd), np.array(gg)
+    good = np.abs(gg - fd) <= 0.05 * np.abs(fd) + 0.01 * np.abs(fd).max()
+    print("\nconfig-4 distribution: agree %d/64" % good.sum())
+    assert good.sum() >= 60
