@@ -199,6 +199,54 @@ gsr_status gsr_forward_depth_first(int variant, int P, const float* pos, const v
                                    float* conic_opacity, int32_t* ranges, const float* bg_color, uint8_t* out_color,
                                    gsr_stream_t stream);
 
+/* ---- ES ("early sorting") steps ------------------------------------------- */
+/* The reference's ES helper operators one by one, with its buffer layouts
+ * (csrc/pybind.cpp:183-330).  Pointers are device pointers except cam_pos
+ * and cam_rot (host).
+ *
+ * gsr_es_pass_a replaces preprocess_es_pass_a{,_half_sh}
+ * (csrc/cuda_rasterizer/preprocess.cu:673-992): the preprocess's features,
+ * plus per Gaussian tiles_per_gauss [P] (hit tiles, 0 when culled),
+ * conic_power_raw [P,4] (conic a, b, c and power), depth_natural [P] (view z,
+ * FLT_MAX when culled) and rect_bounds [P,2] (rect_min, rect_max packed as
+ * x | y << 16).
+ *
+ * gsr_es_depth_sort_and_scan replaces es_depth_sort_and_scan (sort.cu:185-245):
+ * identity = 0..P-1, (depth_sorted, perm) = stable sort of (depth_natural,
+ * identity), tiles_per_gauss_sorted = tiles_per_gauss[perm], cum_offsets_sorted
+ * = its exclusive scan, *total_out (device) = the pair count.  sort_space is
+ * a workspace of at least gsr_workspace_size(P) bytes, scan_space
+ * gsr_es_scan_buffer_size(P) bytes.
+ *
+ * gsr_es_pass_b replaces preprocess_es_pass_b (preprocess.cu:993-1248): for
+ * the s-th Gaussian in depth order, its pairs (tile id y * grid_x + x,
+ * Gaussian index) in tile row-major order from cum_offsets_sorted[s] on.
+ * Pairs at or past `capacity` are not written.
+ *
+ * gsr_es_tile_sort replaces es_tile_sort (sort.cu:247-285): stable sort of the
+ * num pairs by tile id over the bit width of the tile count, and
+ * keys_sorted_out[i] = tile_keys_sorted[i] << 32 for the range search.
+ * sort_space holds at least gsr_workspace_size(num) bytes. */
+gsr_status gsr_es_pass_a(int P, const float* pos, const void* shs, int shs_half, const float* opacity,
+                         const float* cov3d, int width, int height, int block_x, int block_y, const float* cam_pos,
+                         const float* cam_rot, float focal_x, float focal_y, float z_far, float z_near,
+                         float* points_xy, float* rgb_depth, float* conic_opacity, int32_t* tiles_per_gauss,
+                         float* conic_power_raw, float* depth_natural, int32_t* rect_bounds, gsr_stream_t stream);
+size_t gsr_es_scan_buffer_size(int P);
+gsr_status gsr_es_depth_sort_and_scan(int P, const int32_t* tiles_per_gauss, const float* depth_natural,
+                                      uint32_t* identity, uint32_t* perm, float* depth_sorted,
+                                      int32_t* tiles_per_gauss_sorted, int32_t* cum_offsets_sorted,
+                                      int32_t* total_out, void* sort_space, size_t sort_bytes, void* scan_space,
+                                      size_t scan_bytes, gsr_stream_t stream);
+gsr_status gsr_es_pass_b(int P, int width, int height, int block_x, int block_y, const uint32_t* perm,
+                         const int32_t* cum_offsets_sorted, const int32_t* tiles_per_gauss_sorted,
+                         const float* points_xy, const float* conic_power_raw, const int32_t* rect_bounds,
+                         uint32_t* tile_keys_unsorted, uint32_t* values_unsorted, int64_t capacity,
+                         gsr_stream_t stream);
+gsr_status gsr_es_tile_sort(int num, int width, int height, int block_x, int block_y, const uint32_t* tile_keys_unsorted,
+                            const uint32_t* values_unsorted, uint32_t* tile_keys_sorted, uint32_t* values_sorted,
+                            uint64_t* keys_sorted_out, void* sort_space, size_t sort_bytes, gsr_stream_t stream);
+
 /* ---- batched forward ------------------------------------------------------ */
 /* No counterpart in the reference, which renders one view per call.  Views
  * of different scenes and resolutions are rendered by one pass of the

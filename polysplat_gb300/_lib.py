@@ -74,6 +74,12 @@ def _declare(L):
     sig["gsr_depth_first_scratch_size"] = ([i32], sz)
     sig["gsr_forward_depth_first"] = ([i32, i32, P, P, i32, P, P, i32, i32, i32, i32, P, P, f32, f32, f32, f32,
                                        P, P, sz, P, sz, P, P, P, P, i64, P, P, P, P, P, P, P], i32)
+    sig["gsr_es_pass_a"] = ([i32, P, P, i32, P, P, i32, i32, i32, i32, P, P, f32, f32, f32, f32,
+                             P, P, P, P, P, P, P, P], i32)
+    sig["gsr_es_scan_buffer_size"] = ([i32], sz)
+    sig["gsr_es_depth_sort_and_scan"] = ([i32, P, P, P, P, P, P, P, P, P, sz, P, sz, P], i32)
+    sig["gsr_es_pass_b"] = ([i32, i32, i32, i32, i32, P, P, P, P, P, P, P, P, i64, P], i32)
+    sig["gsr_es_tile_sort"] = ([i32, i32, i32, i32, i32, P, P, P, P, P, P, sz, P], i32)
     sig["gsr_camera_matrices"] = ([i32, i32, P, P, f32, f32, f32, f32, P, P], None)
     sig["gsr_profile_begin"] = ([i32], i32)
     sig["gsr_profile_read"] = ([P, i32, i32], i32)

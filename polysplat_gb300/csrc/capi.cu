@@ -184,7 +184,7 @@ static gsr_status preprocess_params(PreprocessParams& p, int P, const float* pos
     if (P > 0 && (!pos || !shs || !opacity || !cov3d || !points_xy || !rgb_depth || !conic_opacity))
         return GSR_INVALID_ARG;
     if (cap > 0 && (!keys || !values)) return GSR_INVALID_ARG;
-    p.df = DepthFirstRecords{nullptr, nullptr, nullptr, nullptr};
+    p.df = DepthFirstRecords{nullptr, nullptr, nullptr, nullptr, 0};
     p.gid_base = 0;
     p.tile_base = 0;
     p.views = nullptr;

@@ -36,6 +36,8 @@ struct DepthFirstRecords {
     uint32_t* dkey;   // [P] depth bit pattern (the key's low word)
     float4* geo;      // [P] conic x, y, z and power (the exact FP32 test inputs)
     int2* rect;       // [P] x0 | x1 << 16, y0 | y1 << 16; bit 31 of .y: queued as massive
+    int ref_layout;   // nonzero: the reference's ES layout instead (rect = (x0 | y0 << 16, x1 | y1 << 16),
+                      // depth FLT_MAX for culled Gaussians; no large-Gaussian queue)
 };
 
 struct PreprocessParams {
@@ -89,6 +91,9 @@ cudaError_t launch_df_emit_small(const PreprocessParams& p, const uint32_t* d_v,
                                  cudaStream_t stream);
 cudaError_t launch_df_emit_massive(const PreprocessParams& p, const uint32_t* offsets, const uint32_t* rank,
                                    uint32_t* tiles, uint32_t* vals, long long cap, cudaStream_t stream);
+cudaError_t launch_es_pass_b(int P, int bx, int by, int gx, const uint32_t* perm, const int32_t* cum,
+                             const int32_t* count_sorted, const float2* xy, const float4* cpr, const int2* rb,
+                             uint32_t* tiles, uint32_t* vals, long long cap, cudaStream_t stream);
 cudaError_t launch_scene_prepare(int P, const float* log_scales, const float* quats, const float* logits,
                                  float* opacity, float* cov3d, cudaStream_t stream);
 

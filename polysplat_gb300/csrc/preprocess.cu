@@ -547,9 +547,15 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const __grid_constan
             if (was_valid) {
                 a.df.dkey[idx] = depth_bits;
                 a.df.geo[idx] = make_float4(conic.x, conic.y, conic.z, power);
-                a.df.rect[idx] = make_int2((int)((uint32_t)rect_min.x | ((uint32_t)rect_max.x << 16)),
-                                           (int)((uint32_t)rect_min.y | ((uint32_t)rect_max.y << 16) |
-                                                 (queued ? 0x80000000u : 0u)));
+                if (a.df.ref_layout)  // (rect_min, rect_max) packed as (x | y << 16), preprocess.cu:975-977
+                    a.df.rect[idx] = make_int2((int)((uint32_t)rect_min.x | ((uint32_t)rect_min.y << 16)),
+                                               (int)((uint32_t)rect_max.x | ((uint32_t)rect_max.y << 16)));
+                else
+                    a.df.rect[idx] = make_int2((int)((uint32_t)rect_min.x | ((uint32_t)rect_max.x << 16)),
+                                               (int)((uint32_t)rect_min.y | ((uint32_t)rect_max.y << 16) |
+                                                     (queued ? 0x80000000u : 0u)));
+            } else if (a.df.ref_layout) {
+                a.df.dkey[idx] = 0x7F7FFFFFu;  // FLT_MAX: culled Gaussians sort last (preprocess.cu:983)
             }
         }
     } else {
@@ -1045,6 +1051,64 @@ cudaError_t launch_df_emit_massive(const PreprocessParams& p, const uint32_t* of
     // the rest of the preprocess region before the counting pass)
     const DfEmit df{offsets, rank, tiles, vals, cap};
     k_emit_massive<kMassiveEmitDf, false><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, df);
+    return cudaGetLastError();
+}
+
+// The reference's ES pass B (preprocess.cu:993-1248): every Gaussian in
+// depth order writes its (tile id, index) pairs from its scanned offset on,
+// from the counting pass's records alone (centre, raw conic + power, packed
+// rectangle).  One warp per Gaussian sweeps its candidate tiles with the
+// counting pass's tile test, so it writes exactly the counted pairs.
+__global__ __launch_bounds__(256) void k_es_pass_b(int P, int bx, int by, int gx, const uint32_t* __restrict__ perm,
+                                                   const int32_t* __restrict__ cum,
+                                                   const int32_t* __restrict__ count_sorted,
+                                                   const float2* __restrict__ xy, const float4* __restrict__ cpr,
+                                                   const int2* __restrict__ rb, uint32_t* __restrict__ tiles,
+                                                   uint32_t* __restrict__ vals, long long cap)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    PreprocessParams pp;
+    pp.bx = bx;
+    pp.by = by;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long s = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); s < P; s += warps) {
+        const int c = __ldg(count_sorted + s);
+        if (c <= 0) continue;
+        const uint32_t gid = __ldg(perm + s);
+        if (gid >= (uint32_t)P) continue;
+        const long long base = __ldg(cum + s);
+        const float2 ctr = __ldg(xy + gid);
+        const float4 cp = __ldg(cpr + gid);
+        const int2 r = __ldg(rb + gid);
+        MassiveEntry me;
+        me.ctr_power_depth = make_float4(ctr.x, ctr.y, cp.w, 0.f);
+        me.conic_gid = make_float4(cp.x, cp.y, cp.z, __uint_as_float(gid));
+        // rect_min / rect_max unpacked as signed 16-bit (preprocess.cu:1043-1048); clamped to the grid
+        const int x0 = max(0, (int)(int16_t)(r.x & 0xFFFF)), y0 = max(0, (int)(int16_t)((r.x >> 16) & 0xFFFF));
+        const int x1 = min(gx, (int)(int16_t)(r.y & 0xFFFF)), y1 = (int)(int16_t)((r.y >> 16) & 0xFFFF);
+        me.rect = make_int4(x0, max(x0, x1), y0, max(y0, y1));
+        uint32_t wpos = 0;
+        sweep_warp(me, pp, lane, [&](bool v, int x, int y) {
+            const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
+            if (v) {
+                const long long pos = base + wpos + __popc(m & lanemask_lt());
+                if (pos >= 0 && pos < cap && wpos + __popc(m & lanemask_lt()) < (uint32_t)c) {
+                    tiles[pos] = (uint32_t)(y * gx + x);
+                    vals[pos] = gid;
+                }
+            }
+            wpos += __popc(m);
+        });
+    }
+}
+
+cudaError_t launch_es_pass_b(int P, int bx, int by, int gx, const uint32_t* perm, const int32_t* cum,
+                             const int32_t* count_sorted, const float2* xy, const float4* cpr, const int2* rb,
+                             uint32_t* tiles, uint32_t* vals, long long cap, cudaStream_t stream)
+{
+    if (P <= 0) return cudaSuccess;
+    const int grid = std::min(div_up(P, 8), device_sm_count() * 8);
+    k_es_pass_b<<<grid, 256, 0, stream>>>(P, bx, by, gx, perm, cum, count_sorted, xy, cpr, rb, tiles, vals, cap);
     return cudaGetLastError();
 }
 

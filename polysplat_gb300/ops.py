@@ -13,9 +13,12 @@ Differences a caller can observe, all deliberate:
   ``csrc/pybind.cpp:1124-1134``);
 * ``get_sort_buffer_size(n)`` returns the size of this library's workspace
   (radix-sort ping-pong buffers, look-back state, tile queue and status word);
-* the ES ("early sorting") and tile-reordering helpers are provided for API
-  completeness; renders that take tile orders produce the same image as the
-  plain persistent render because tile order never changes a tile's result.
+* the ES ("early sorting") helpers fill the reference's buffers with the
+  reference's meanings; their scan scratch is this library's (see
+  ``get_es_scan_buffer_size``) and the sort scratch is the workspace;
+* the tile-reordering helpers are provided for API completeness; renders that
+  take tile orders produce the same image as the plain persistent render
+  because tile order never changes a tile's result.
 """
 from __future__ import annotations
 
@@ -523,20 +526,119 @@ def compute_tile_order_packed_morton(tile_ranges_buf, total_tiles, x_blocks, til
 # ---------------------------------------------------------------------------
 # ES ("early sorting") two-pass helpers (csrc/pybind.cpp:183-330)
 
-def _es_unavailable(*_a, **_k):
-    raise NotImplementedError("the ES two-pass helpers are not provided by this library; the fused forward "
-                              "always uses the single-pass tile-key pipeline")
+def _es_pass_a(half, orig_points, shs, opacities, cov3Ds, width, height, block_x, block_y, position, rotation,
+               focal_x, focal_y, zFar, zNear, points_xy, rgb_depth, conic_opacity, tiles_per_gauss,
+               conic_power_raw, depth_natural, rect_bounds):
+    pos = _dev(orig_points, "orig_points", torch.float32)
+    sh = _dev(shs, "shs", torch.float16 if half else torch.float32)
+    op = _dev(opacities, "opacities", torch.float32)
+    cov = _dev(cov3Ds, "cov3Ds", torch.float32)
+    for t, n in ((points_xy, "points_xy"), (rgb_depth, "rgb_depth"), (conic_opacity, "conic_opacity"),
+                 (conic_power_raw, "conic_power_raw"), (depth_natural, "depth_natural")):
+        _dev(t, n, torch.float32)
+    _dev(tiles_per_gauss, "tiles_per_gauss", torch.int32)
+    _dev(rect_bounds, "rect_bounds", torch.int32)
+    P = op.numel()
+    for t, per, n in ((tiles_per_gauss, 1, "tiles_per_gauss"), (conic_power_raw, 4, "conic_power_raw"),
+                      (depth_natural, 1, "depth_natural"), (rect_bounds, 2, "rect_bounds"),
+                      (points_xy, 2, "points_xy"), (rgb_depth, 4, "rgb_depth"), (conic_opacity, 4, "conic_opacity")):
+        if t.numel() < per * P:
+            raise GsrError(_lib.GSR_INVALID_ARG, "preprocess_es_pass_a: %s holds fewer than %d x %d values"
+                           % (n, P, per))
+    st = lib().gsr_es_pass_a(P, _ptr(pos), _ptr(sh), 1 if half else 0, _ptr(op), _ptr(cov), int(width),
+                             int(height), int(block_x), int(block_y), _host_floats(position, 3, "position"),
+                             _host_floats(rotation, 9, "rotation"), float(focal_x), float(focal_y), float(zFar),
+                             float(zNear), _ptr(points_xy), _ptr(rgb_depth), _ptr(conic_opacity),
+                             _ptr(tiles_per_gauss), _ptr(conic_power_raw), _ptr(depth_natural), _ptr(rect_bounds),
+                             _stream(op.device))
+    check(st, "preprocess_es_pass_a")
 
 
-preprocess_es_pass_a = _es_unavailable
-preprocess_es_pass_a_half_sh = _es_unavailable
-preprocess_es_pass_b = _es_unavailable
-es_depth_sort_and_scan = _es_unavailable
-es_tile_sort = _es_unavailable
+def preprocess_es_pass_a(orig_points, shs, opacities, cov3Ds, width, height, block_x, block_y, position, rotation,
+                         focal_x, focal_y, zFar, zNear, points_xy, rgb_depth, conic_opacity, tiles_per_gauss,
+                         conic_power_raw, depth_natural, rect_bounds, /):
+    """ES pass A (csrc/pybind.cpp:183-215): the preprocess without key
+    emission; per Gaussian its hit-tile count, raw conic and power, view depth
+    (FLT_MAX when culled) and tile rectangle packed as x | y << 16."""
+    _es_pass_a(False, orig_points, shs, opacities, cov3Ds, width, height, block_x, block_y, position, rotation,
+               focal_x, focal_y, zFar, zNear, points_xy, rgb_depth, conic_opacity, tiles_per_gauss,
+               conic_power_raw, depth_natural, rect_bounds)
+
+
+def preprocess_es_pass_a_half_sh(orig_points, shs_half, opacities, cov3Ds, width, height, block_x, block_y,
+                                 position, rotation, focal_x, focal_y, zFar, zNear, points_xy, rgb_depth,
+                                 conic_opacity, tiles_per_gauss, conic_power_raw, depth_natural, rect_bounds, /):
+    _es_pass_a(True, orig_points, shs_half, opacities, cov3Ds, width, height, block_x, block_y, position, rotation,
+               focal_x, focal_y, zFar, zNear, points_xy, rgb_depth, conic_opacity, tiles_per_gauss,
+               conic_power_raw, depth_natural, rect_bounds)
 
 
 def get_es_scan_buffer_size(P, /):
-    return 4 * int(P) + 256
+    return int(lib().gsr_es_scan_buffer_size(int(P)))
+
+
+def es_depth_sort_and_scan(P, tiles_per_gauss, depth_natural, identity_buf, perm_buf, depth_sorted_buf,
+                           tiles_per_gauss_sorted_buf, cum_offsets_sorted_buf, total_num_rendered_out,
+                           cub_sort_scratch, cub_scan_scratch, /):
+    """Stable sort of the Gaussians by view depth, their tile counts in that
+    order and its exclusive scan; the total lands in total_num_rendered_out[0]
+    on the device (csrc/pybind.cpp:249-292, sort.cu:185-245)."""
+    P = int(P)
+    ts = [_dev(tiles_per_gauss, "tiles_per_gauss", torch.int32), _dev(depth_natural, "depth_natural", torch.float32),
+          _dev(identity_buf, "identity_buf", torch.int32), _dev(perm_buf, "perm_buf", torch.int32),
+          _dev(depth_sorted_buf, "depth_sorted_buf", torch.float32),
+          _dev(tiles_per_gauss_sorted_buf, "tiles_per_gauss_sorted_buf", torch.int32),
+          _dev(cum_offsets_sorted_buf, "cum_offsets_sorted_buf", torch.int32)]
+    if any(t.numel() < P for t in ts):
+        raise GsrError(_lib.GSR_INVALID_ARG, "es_depth_sort_and_scan: a per-Gaussian buffer holds fewer than %d" % P)
+    tot = _dev(total_num_rendered_out, "total_num_rendered_out", torch.int32)
+    ws = _dev(cub_sort_scratch, "cub_sort_scratch")
+    sc = _dev(cub_scan_scratch, "cub_scan_scratch")
+    st = lib().gsr_es_depth_sort_and_scan(P, *[_ptr(t) for t in ts], _ptr(tot), _ptr(ws),
+                                          ws.numel() * ws.element_size(), _ptr(sc), sc.numel() * sc.element_size(),
+                                          _stream(tot.device))
+    check(st, "es_depth_sort_and_scan")
+
+
+def preprocess_es_pass_b(P, width, height, block_x, block_y, perm, cum_offsets_sorted, tiles_per_gauss_sorted,
+                         points_xy, conic_power_raw, rect_bounds, tile_keys_unsorted, gauss_values_unsorted, /):
+    """ES pass B (csrc/pybind.cpp:217-247): the (tile id, index) pairs of the
+    Gaussians in depth order, each Gaussian's from its scanned offset on.
+    Pairs past the output buffers are dropped (the count is known from the
+    scan's total)."""
+    P = int(P)
+    ts = [_dev(perm, "perm", torch.int32), _dev(cum_offsets_sorted, "cum_offsets_sorted", torch.int32),
+          _dev(tiles_per_gauss_sorted, "tiles_per_gauss_sorted", torch.int32)]
+    xy = _dev(points_xy, "points_xy", torch.float32)
+    cpr = _dev(conic_power_raw, "conic_power_raw", torch.float32)
+    rb = _dev(rect_bounds, "rect_bounds", torch.int32)
+    if any(t.numel() < P for t in ts) or xy.numel() < 2 * P or cpr.numel() < 4 * P or rb.numel() < 2 * P:
+        raise GsrError(_lib.GSR_INVALID_ARG, "preprocess_es_pass_b: a per-Gaussian buffer holds fewer than %d" % P)
+    tu = _dev(tile_keys_unsorted, "tile_keys_unsorted", torch.int32)
+    vu = _dev(gauss_values_unsorted, "gauss_values_unsorted", torch.int32)
+    cap = min(tu.numel(), vu.numel())
+    st = lib().gsr_es_pass_b(P, int(width), int(height), int(block_x), int(block_y), *[_ptr(t) for t in ts],
+                             _ptr(xy), _ptr(cpr), _ptr(rb), _ptr(tu), _ptr(vu), cap, _stream(tu.device))
+    check(st, "preprocess_es_pass_b")
+
+
+def es_tile_sort(num_rendered, width, height, block_x, block_y, tile_keys_unsorted, gauss_values_unsorted,
+                 tile_keys_sorted, gauss_values_sorted, gaussian_keys_sorted_out, cub_sort_scratch, /):
+    """Stable sort of the pairs by 32-bit tile id over the id's bit width, and
+    the 64-bit keys tile << 32 for the range search (csrc/pybind.cpp:294-330,
+    sort.cu:247-285)."""
+    n = int(num_rendered)
+    ts = [_dev(tile_keys_unsorted, "tile_keys_unsorted", torch.int32),
+          _dev(gauss_values_unsorted, "gauss_values_unsorted", torch.int32),
+          _dev(tile_keys_sorted, "tile_keys_sorted", torch.int32),
+          _dev(gauss_values_sorted, "gauss_values_sorted", torch.int32)]
+    ko = _dev(gaussian_keys_sorted_out, "gaussian_keys_sorted_out", torch.int64)
+    if any(t.numel() < n for t in ts) or ko.numel() < n:
+        raise GsrError(_lib.GSR_OVERFLOW, "es_tile_sort", n)
+    ws = _dev(cub_sort_scratch, "cub_sort_scratch")
+    st = lib().gsr_es_tile_sort(n, int(width), int(height), int(block_x), int(block_y), *[_ptr(t) for t in ts],
+                                _ptr(ko), _ptr(ws), ws.numel() * ws.element_size(), _stream(ko.device))
+    check(st, "es_tile_sort")
 
 
 # ---------------------------------------------------------------------------
