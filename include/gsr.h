@@ -48,6 +48,8 @@ typedef enum {
     GSR_RENDER_DEFAULT = 2,           /* render_16x16 / renderCUDA (render.cu:2176): ranges in-kernel, cadence 2 */
     GSR_RENDER_RANGES_CADENCE2 = 3,   /* preranges variants with per-pair exit checks */
     GSR_RENDER_DT = 4,                /* ..._lite_dt (render.cu:1871-2018): skips power < log2(1/255), cadence 8 */
+    GSR_RENDER_SPLIT = 5,             /* render_{16,24,32}x16_split (render.cu:3859-4357): ranges in-kernel, cadence 2,
+                                         top and bottom 8-row halves stop independently; 16-row tiles only */
 } gsr_render_variant;
 
 /* Library version and a check that a CUDA device of compute capability 10.3
@@ -246,6 +248,28 @@ gsr_status gsr_es_pass_b(int P, int width, int height, int block_x, int block_y,
 gsr_status gsr_es_tile_sort(int num, int width, int height, int block_x, int block_y, const uint32_t* tile_keys_unsorted,
                             const uint32_t* values_unsorted, uint32_t* tile_keys_sorted, uint32_t* values_sorted,
                             uint64_t* keys_sorted_out, void* sort_space, size_t sort_bytes, gsr_stream_t stream);
+
+/* ---- tile order (reordered-render helpers) --------------------------------- */
+/* gsr_tile_order replaces compute_tile_order, compute_tile_order_packed and
+ * compute_tile_order_packed_morton (render.cu:6959-7087; pybind.cpp:461-553):
+ * tile_ids[t] = t; tile_order = the tiles by descending sort key, equal keys
+ * in index order; tile_counts = the sorted keys.  The key is the tile's pair
+ * count (ranges[t].y - ranges[t].x), or with morton_bucket > 0
+ * (min(count / morton_bucket, 0xFFFF) << 16) | (0xFFFF - Morton(x, y) & 0xFFFF)
+ * (render.cu:4496-4520).  With tile_desc != NULL, tile_desc[i] = {col, row,
+ * start, end} of tile_order[i]; with zigzag_group > 1 the odd groups of
+ * zigzag_group positions take their slice of the order backwards
+ * (render.cu:4813-4866).  temp holds gsr_tile_order_temp_size(total_tiles)
+ * bytes (= get_tile_order_sort_temp_size). */
+size_t gsr_tile_order_temp_size(int total_tiles);
+gsr_status gsr_tile_order(const int32_t* tile_ranges, int total_tiles, int x_blocks, int morton_bucket,
+                          int zigzag_group, int32_t* tile_desc, uint32_t* tile_order, uint32_t* tile_counts,
+                          uint32_t* tile_ids, void* temp, size_t temp_bytes, gsr_stream_t stream);
+/* Per-tile ranges back from descriptors: ranges[row * x_blocks + col] =
+ * {start, end} (what the reordered renders read; the tile order never
+ * changes a tile's pixels). */
+gsr_status gsr_tile_desc_ranges(const int32_t* tile_desc, int total_tiles, int x_blocks, int32_t* tile_ranges,
+                                gsr_stream_t stream);
 
 /* ---- batched forward ------------------------------------------------------ */
 /* No counterpart in the reference, which renders one view per call.  Views

@@ -207,3 +207,44 @@ def image_fp64(means, log_scales, quats, logits, shs, cam, bg=(0.0, 0.0, 0.0), c
                                 _p(tgt) if tgt is not None else None, _p(img), nthreads or nthreads_default())
     return float(loss), img
 
+
+
+def _spread16(v):
+    v = v.astype(np.uint32) & np.uint32(0xFFFF)
+    for shift, mask in ((8, 0x00FF00FF), (4, 0x0F0F0F0F), (2, 0x33333333), (1, 0x55555555)):
+        v = (v | (v << np.uint32(shift))) & np.uint32(mask)
+    return v
+
+
+def tile_order(ranges, x_blocks, morton_bucket=0, zigzag=0):
+    """Tile reordering of the reference's reordered renders, in numpy.
+
+    Sort key per tile t: its pair count ranges[t,1] - ranges[t,0]
+    (extractTileCounts, render.cu:4414-4426), or with morton_bucket > 0
+    (min(count // bucket, 0xFFFF) << 16) | (0xFFFF - Morton(x, y) & 0xFFFF)
+    (extractTileCountsMorton, render.cu:4496-4520).  Stable descending sort
+    of (key, tile id) (cub SortPairsDescending, render.cu:6973-6977).
+    Descriptors {col, row, start, end} in that order (gatherTileDesc,
+    render.cu:4813-4831); with zigzag > 1 odd groups of `zigzag` positions
+    read their slice backwards (gatherTileDescZigzag, render.cu:4838-4866).
+
+    Returns (order, sorted_keys, ids, desc) as uint32/int32 arrays."""
+    r = np.asarray(ranges, dtype=np.int64).reshape(-1, 2)
+    T = r.shape[0]
+    key = ((r[:, 1] - r[:, 0]) & 0xFFFFFFFF).astype(np.uint32)
+    t = np.arange(T, dtype=np.int64)
+    if morton_bucket > 0:
+        bucket = np.minimum(key // np.uint32(morton_bucket), np.uint32(0xFFFF)).astype(np.uint32)
+        morton = (_spread16(t % x_blocks) | (_spread16(t // x_blocks) << np.uint32(1))) & np.uint32(0xFFFF)
+        key = (bucket << np.uint32(16)) | (np.uint32(0xFFFF) - morton)
+    order = np.argsort(-key.astype(np.int64), kind="stable").astype(np.uint32)
+    src = t.copy()
+    if zigzag > 1:
+        g = t // zigzag
+        base = g * zigzag
+        length = np.minimum(base + zigzag, T) - base
+        src = np.where(g % 2 == 1, base + (length - 1 - (t - base)), t)
+        src = np.minimum(src, T - 1)
+    ids = order[src].astype(np.int64)
+    desc = np.stack([ids % x_blocks, ids // x_blocks, r[ids, 0], r[ids, 1]], axis=1).astype(np.int32)
+    return order, key[order], t.astype(np.uint32), desc

@@ -139,8 +139,10 @@ class Pipeline:
 
 
 def render(which, M, W, H, xy, rgbd, con, keys, vals, ranges, bg, out):
-    """which: 'lite' (ranges), 'fused' (keys), 'default' (keys)."""
-    code = {"lite": 0, "fused": 1, "default": 2}[which]
+    """which: 'lite' (ranges), 'fused' (keys), 'default', '32x16', '32x32',
+    'unroll2', 'split16', 'split24', 'split32' (keys)."""
+    code = {"lite": 0, "fused": 1, "default": 2, "32x16": 3, "32x32": 4, "unroll2": 5, "split16": 6,
+            "split24": 7, "split32": 8}[which]
     rc = lib().ref_render(code, int(M), int(W), int(H), xy.data_ptr(), rgbd.data_ptr(), con.data_ptr(),
                           keys.data_ptr() if keys is not None else None, vals.data_ptr(),
                           ranges.data_ptr() if ranges is not None else None, _f(bg, 3), out.data_ptr(),

@@ -9,7 +9,10 @@
 // the same GB300:
 //   preprocessCUDA            csrc/cuda_rasterizer/preprocess.cu:313, launch :1268-1329
 //   computeTileRanges         render.cu:3510, launch :6812-6824
-//   renderCUDA<16,16,2,4>     render.cu:2176, launch :4365-4385
+//   renderCUDA<16,16,2,4>     render.cu:2176, launch :4365-4385 (also <32,16,4,4>,
+//                             <32,32,4,8> and the unroll2 form, render.cu:6917-6957)
+//   renderCUDAWarpSplit<16|24,16,..,2>  render.cu:4115, launch :4386-4409
+//   renderCUDA32x16Split      render.cu:3859, launch :6927-6946
 //   renderCUDA_preranges_smem_persistent_lite<16,16,2,4>       render.cu:1717, launch :6537-6573
 //   renderCUDA_preranges_smem_persistent_lite_fused<16,16,2,4> render.cu:2026, launch :6616-6652
 // The reference's sort.cu does not compile against CUDA 13's CCCL (its
@@ -173,7 +176,8 @@ int ref_tile_ranges(int M, const void* keys, int tiles, void* ranges, void* stre
     return r == CUDA_SUCCESS ? 0 : 40 + (int)r;
 }
 
-// which: 0 = persistent lite (ranges), 1 = persistent lite fused (keys), 2 = default renderCUDA (keys)
+// which: 0 = persistent lite (ranges), 1 = persistent lite fused (keys), 2 = default renderCUDA (keys),
+// 3-8 = the other one-block-per-tile renders (keys; see the table below)
 int ref_render(int which, int M, int W, int H, const void* xy, const void* rgbd, const void* con, const void* keys,
                const void* vals, const void* ranges, const float* bg3, void* out, void* stream)
 {
@@ -207,13 +211,29 @@ int ref_render(int which, int M, int W, int H, const void* xy, const void* rgbd,
                 r = cuLaunchKernel(f, grid, 1, 1, 8, 4, 1, 0, (CUstream)stream, args, nullptr);
             }
         }
-    } else if (which == 2) {
-        CUfunction f = find(m, "10renderCUDAILi16ELi16ELi2ELi4ELb0ELb0E");
+    } else if (which >= 2 && which <= 8) {
+        // one block per tile, ranges searched in the keys (render.cu:4365-4409, 6897-6946)
+        struct Shape {
+            const char* needle;
+            int bx, by, tx, ty;
+        };
+        static const Shape shapes[] = {
+            {"10renderCUDAILi16ELi16ELi2ELi4ELb0ELb0E", 16, 16, 8, 4},         // 2: render_16x16
+            {"10renderCUDAILi32ELi16ELi4ELi4ELb0ELb0E", 32, 16, 8, 4},         // 3: render_32x16
+            {"10renderCUDAILi32ELi32ELi4ELi8ELb0ELb0E", 32, 32, 8, 4},         // 4: render_32x32
+            {"10renderCUDAILi16ELi16ELi2ELi4ELb1ELb0E", 16, 16, 8, 4},         // 5: render_16x16_unroll2
+            {"19renderCUDAWarpSplitILi16ELi16ELi2ELi2ELi2E", 16, 16, 8, 8},    // 6: render_16x16_split
+            {"19renderCUDAWarpSplitILi24ELi16ELi3ELi2ELi2E", 24, 16, 8, 8},    // 7: render_24x16_split
+            {"20renderCUDA32x16Split", 32, 16, 16, 4},                          // 8: render_32x16_split
+        };
+        const Shape& sh = shapes[which - 2];
+        CUfunction f = find(m, sh.needle);
         if (f) {
+            const int gx = (W + sh.bx - 1) / sh.bx, gy = (H + sh.by - 1) / sh.by;
             LoadInfo info = make_load_info(vals, (const float*)xy, (const float*)rgbd, (const float*)con);
-            void* args[] = {(void*)&keys, &M, (void*)&vals, &W, &H, (void*)&x_blocks, (void*)&xy, (void*)&rgbd,
+            void* args[] = {(void*)&keys, &M, (void*)&vals, &W, &H, (void*)&gx, (void*)&xy, (void*)&rgbd,
                             (void*)&con,  &info, bg, &out};
-            r = cuLaunchKernel(f, x_blocks, y_blocks, 1, 8, 4, 1, 0, (CUstream)stream, args, nullptr);
+            r = cuLaunchKernel(f, gx, gy, 1, sh.tx, sh.ty, 1, 0, (CUstream)stream, args, nullptr);
         }
     }
     int rc = r == CUDA_SUCCESS ? 0 : 60 + (int)r;

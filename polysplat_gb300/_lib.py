@@ -23,6 +23,7 @@ RENDER_PERSISTENT_FUSED = 1
 RENDER_DEFAULT = 2
 RENDER_RANGES_CADENCE2 = 3
 RENDER_DT = 4
+RENDER_SPLIT = 5
 
 
 class GsrError(RuntimeError):
@@ -80,6 +81,9 @@ def _declare(L):
     sig["gsr_es_depth_sort_and_scan"] = ([i32, P, P, P, P, P, P, P, P, P, sz, P, sz, P], i32)
     sig["gsr_es_pass_b"] = ([i32, i32, i32, i32, i32, P, P, P, P, P, P, P, P, i64, P], i32)
     sig["gsr_es_tile_sort"] = ([i32, i32, i32, i32, i32, P, P, P, P, P, P, sz, P], i32)
+    sig["gsr_tile_order_temp_size"] = ([i32], sz)
+    sig["gsr_tile_order"] = ([P, i32, i32, i32, i32, P, P, P, P, P, sz, P], i32)
+    sig["gsr_tile_desc_ranges"] = ([P, i32, i32, P, P], i32)
     sig["gsr_camera_matrices"] = ([i32, i32, P, P, f32, f32, f32, f32, P, P], None)
     sig["gsr_profile_begin"] = ([i32], i32)
     sig["gsr_profile_read"] = ([P, i32, i32], i32)

@@ -332,7 +332,7 @@ static gsr_status render_impl(int variant, int num, const int32_t* d_num, long l
     if (!workspace || !out_color || !bg_color || width <= 0 || height <= 0 || !valid_tile_shape(block_x, block_y))
         return GSR_INVALID_ARG;
     if (render_needs_ranges(variant) ? !ranges : (!keys_sorted && !ranges)) return GSR_INVALID_ARG;
-    if (variant < 0 || variant > GSR_RENDER_DT) return GSR_INVALID_ARG;
+    if (variant < 0 || variant > GSR_RENDER_SPLIT) return GSR_INVALID_ARG;
     RenderArgs a;
     a.variant = variant;
     a.num = num;
@@ -425,7 +425,7 @@ gsr_status gsr_forward_depth_first(int variant, int P, const float* pos, const v
 {
     cudaStream_t s = (cudaStream_t)stream;
     if (!workspace || !curr_offset || !scene_scratch || !valid_tile_shape(block_x, block_y)) return GSR_INVALID_ARG;
-    if (variant < 0 || variant > GSR_RENDER_DT) return GSR_INVALID_ARG;
+    if (variant < 0 || variant > GSR_RENDER_SPLIT) return GSR_INVALID_ARG;
     if (workspace_bytes < sort_workspace_bytes(key_capacity) || key_capacity >= (1LL << 30)) return GSR_INVALID_ARG;
     if (P < 0 || scene_scratch_bytes < df_scratch_bytes(P)) return GSR_INVALID_ARG;
     if (key_capacity > 0 && (!tiles_unsorted || !values_unsorted || !tiles_sorted || !values_sorted))

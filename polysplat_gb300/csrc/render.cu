@@ -228,7 +228,11 @@ __device__ __forceinline__ void shade(float (&C)[TY][TX][3], float (&T)[TY][TX],
 }
 
 // RANGE_MODE 0: ranges[] given; 1: warp search in the sorted keys.
-template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA, bool BATCH>
+// EXIT 0: the tile stops when all its pixels are saturated; EXIT 1: the top
+// and bottom halves (8 rows each, lanes 0-15 and 16-31) stop independently,
+// as the reference's two-warp split kernels do (renderCUDAWarpSplit,
+// render.cu:4115-4357; renderCUDA32x16Split, render.cu:3859-4106).
+template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA, bool BATCH, int EXIT = 0>
 __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams p)
 {
     constexpr int TX = BX / 8, TY = BY / 4;
@@ -302,6 +306,7 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
             int cur = 0;
             stage_batch<TMA>(R, 0, p, start, min(kBatch, total), lane, bad);
             int processed = 0;
+            bool half_done = false;  // EXIT 1: this lane's half has stopped
             for (int pos = start; pos < end; pos += kBatch) {
                 const int bsize = min(kBatch, end - pos);
                 const int npos = pos + kBatch;
@@ -317,7 +322,8 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
                     const float4 cd = R.rgbd[cur][g];
                     const float4 x2 = R.xy2[cur][g];
                     const float2 xy = R.sel[cur][g] ? make_float2(x2.z, x2.w) : make_float2(x2.x, x2.y);
-                    shade<TX, TY, SHADER, DT>(C, T, ox, oy, cb, rb, xy, co, make_float3(cd.x, cd.y, cd.z));
+                    if (EXIT == 0 || !half_done)
+                        shade<TX, TY, SHADER, DT>(C, T, ox, oy, cb, rb, xy, co, make_float3(cd.x, cd.y, cd.z));
                     ++processed;
                     if (processed % CADENCE == 0) {
                         bool sat = true;
@@ -325,9 +331,19 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
                         for (int i = 0; i < TY; i++)
 #pragma unroll
                             for (int j = 0; j < TX; j++) sat = sat && T[i][j] < 0.0001f;
-                        if (__all_sync(GSR_FULL_MASK, sat)) {
-                            exit_now = true;
-                            break;
+                        if (EXIT == 0) {
+                            if (__all_sync(GSR_FULL_MASK, sat)) {
+                                exit_now = true;
+                                break;
+                            }
+                        } else {
+                            const unsigned m = __ballot_sync(GSR_FULL_MASK, sat);
+                            const bool lo = (m & 0xFFFFu) == 0xFFFFu, hi = (m >> 16) == 0xFFFFu;
+                            if (lo && hi) {
+                                exit_now = true;
+                                break;
+                            }
+                            half_done = half_done || (lane < 16u ? lo : hi);
                         }
                     }
                 }
@@ -364,10 +380,11 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
     }
 }
 
-template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA, bool BATCH = false>
+template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA, bool BATCH = false,
+          int EXIT = 0>
 cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
 {
-    auto kern = k_render<BX, BY, CADENCE, SHADER, DT, RANGE_MODE, TMA, BATCH>;
+    auto kern = k_render<BX, BY, CADENCE, SHADER, DT, RANGE_MODE, TMA, BATCH, EXIT>;
     static int per_sm = 0;
     if (per_sm == 0) {
         int b = 0;
@@ -410,6 +427,10 @@ cudaError_t dispatch_shape(int variant, bool tma, const RenderParams& p, cudaStr
     case GSR_RENDER_DT:
         return tma ? launch_variant<BX, BY, 8, 0, true, 0, true>(p, stream)
                    : launch_variant<BX, BY, 8, 0, true, 0, false>(p, stream);
+    case GSR_RENDER_SPLIT:  // axis-shared shader at every tile width, per-half exit
+        if (BY != 16) return cudaErrorInvalidValue;
+        if (ranges) return launch_variant<BX, BY, 2, 0, false, 0, false, false, 1>(p, stream);
+        return launch_variant<BX, BY, 2, 0, false, 1, false, false, 1>(p, stream);
     default:
         return cudaErrorInvalidValue;
     }

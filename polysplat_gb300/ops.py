@@ -337,13 +337,13 @@ def render_16x16_unroll2(num_rendered, width, height, points_xy, rgb_depth, coni
 
 def render_16x16_split(num_rendered, width, height, points_xy, rgb_depth, conic_opacity, gaussian_keys_sorted,
                        gaussian_values_sorted, bg_color, out_color, /):
-    _render(R.RENDER_DEFAULT, num_rendered, width, height, points_xy, rgb_depth, conic_opacity,
+    _render(R.RENDER_SPLIT, num_rendered, width, height, points_xy, rgb_depth, conic_opacity,
             gaussian_keys_sorted, gaussian_values_sorted, None, bg_color, out_color)
 
 
 def render_24x16_split(num_rendered, width, height, points_xy, rgb_depth, conic_opacity, gaussian_keys_sorted,
                        gaussian_values_sorted, bg_color, out_color, /):
-    _render(R.RENDER_DEFAULT, num_rendered, width, height, points_xy, rgb_depth, conic_opacity,
+    _render(R.RENDER_SPLIT, num_rendered, width, height, points_xy, rgb_depth, conic_opacity,
             gaussian_keys_sorted, gaussian_values_sorted, None, bg_color, out_color, 24, 16)
 
 
@@ -355,7 +355,7 @@ def render_32x16(num_rendered, width, height, points_xy, rgb_depth, conic_opacit
 
 def render_32x16_split(num_rendered, width, height, points_xy, rgb_depth, conic_opacity, gaussian_keys_sorted,
                        gaussian_values_sorted, bg_color, out_color, /):
-    _render(R.RENDER_DEFAULT, num_rendered, width, height, points_xy, rgb_depth, conic_opacity,
+    _render(R.RENDER_SPLIT, num_rendered, width, height, points_xy, rgb_depth, conic_opacity,
             gaussian_keys_sorted, gaussian_values_sorted, None, bg_color, out_color, 32, 16)
 
 
@@ -412,13 +412,14 @@ def render_16x16_preranges_smem_v2(num_rendered, width, height, points_xy, rgb_d
 
 
 def _desc_to_ranges(tile_desc_buf, width, height):
-    """int4 tile descriptors {col,row,start,end} -> per-tile [start,end)."""
+    """int4 tile descriptors {col, row, start, end} -> per-tile [start, end)."""
     T = _tiles(width, height, 16, 16)
-    gx = (width + 15) // 16
-    d = tile_desc_buf.view(-1, 4)[:T].long()
-    ranges = torch.zeros((T, 2), dtype=torch.int32, device=tile_desc_buf.device)
-    tid = d[:, 1] * gx + d[:, 0]
-    ranges[tid] = d[:, 2:4].int()
+    d = _dev(tile_desc_buf, "tile_desc_buf", torch.int32)
+    if d.numel() < 4 * T:
+        raise GsrError(_lib.GSR_INVALID_ARG, "tile_desc_buf holds fewer than %d descriptors" % T)
+    ranges = torch.zeros((T, 2), dtype=torch.int32, device=d.device)
+    check(lib().gsr_tile_desc_ranges(_ptr(d), T, (int(width) + 15) // 16, _ptr(ranges), _stream(d.device)),
+          "tile descriptors")
     return ranges
 
 
@@ -487,40 +488,51 @@ def render_16x16_topk_smem_persistent_v2(num_rendered, width, height, points_xy,
 # tile-order helpers (ablations; the persistent queue makes them unnecessary)
 
 def get_tile_order_sort_temp_size(total_tiles, /):
-    return int(lib().gsr_workspace_size(int(total_tiles)))
+    return int(lib().gsr_tile_order_temp_size(int(total_tiles)))
 
 
-def _tile_counts(tile_ranges_buf, total_tiles):
-    r = tile_ranges_buf.view(-1, 2)[:total_tiles]
-    return (r[:, 1] - r[:, 0]).clamp_min(0)
+def _tile_order(tile_ranges_buf, total_tiles, x_blocks, morton_bucket, zigzag, tile_desc_buf, tile_order,
+                tile_counts_buf, tile_ids_buf, sort_temp, where):
+    T = int(total_tiles)
+    r = _dev(tile_ranges_buf, "tile_ranges_buf", torch.int32)
+    outs = [_dev(tile_order, "tile_order", torch.int32), _dev(tile_counts_buf, "tile_counts_buf", torch.int32),
+            _dev(tile_ids_buf, "tile_ids_buf", torch.int32)]
+    if r.numel() < 2 * T or any(t.numel() < T for t in outs):
+        raise GsrError(_lib.GSR_INVALID_ARG, "%s: a tile buffer holds fewer than %d tiles" % (where, T))
+    desc = None
+    if tile_desc_buf is not None:
+        desc = _dev(tile_desc_buf, "tile_desc_buf", torch.int32)
+        if desc.numel() < 4 * T:
+            raise GsrError(_lib.GSR_INVALID_ARG, "%s: tile_desc_buf holds fewer than %d descriptors" % (where, T))
+    tmp = _dev(sort_temp, "sort_temp")
+    st = lib().gsr_tile_order(_ptr(r), T, int(x_blocks), int(morton_bucket), int(zigzag),
+                              _ptr(desc) if desc is not None else None, *[_ptr(t) for t in outs], _ptr(tmp),
+                              tmp.numel() * tmp.element_size(), _stream(r.device))
+    check(st, where)
 
 
 def compute_tile_order(tile_ranges_buf, total_tiles, tile_order, tile_counts_buf, tile_ids_buf, sort_temp, /):
-    T = int(total_tiles)
-    c = _tile_counts(tile_ranges_buf, T)
-    order = torch.sort(c, descending=True, stable=True).indices.int()
-    tile_order[:T].copy_(order)
-    tile_counts_buf[:T].copy_(c.int())
-    tile_ids_buf[:T].copy_(torch.arange(T, device=c.device, dtype=torch.int32))
+    """Tiles by descending pair count, ties in index order (render.cu:6959-6979)."""
+    _tile_order(tile_ranges_buf, total_tiles, 1, 0, 0, None, tile_order, tile_counts_buf, tile_ids_buf, sort_temp,
+                "compute_tile_order")
 
 
 def compute_tile_order_packed(tile_ranges_buf, total_tiles, x_blocks, tile_desc_buf, tile_order, tile_counts_buf,
                               tile_ids_buf, sort_temp, zigzag_group_size=0, /):
-    T = int(total_tiles)
-    compute_tile_order(tile_ranges_buf, T, tile_order, tile_counts_buf, tile_ids_buf, sort_temp)
-    o = tile_order[:T].long()
-    r = tile_ranges_buf.view(-1, 2)[:T]
-    d = tile_desc_buf.view(-1, 4)
-    d[:T, 0] = (o % int(x_blocks)).int()
-    d[:T, 1] = (o // int(x_blocks)).int()
-    d[:T, 2:4] = r[o]
+    """The same order plus packed {col, row, start, end} descriptors,
+    zig-zagged over groups when zigzag_group_size > 1 (render.cu:6981-7016)."""
+    _tile_order(tile_ranges_buf, total_tiles, x_blocks, 0, zigzag_group_size, tile_desc_buf, tile_order,
+                tile_counts_buf, tile_ids_buf, sort_temp, "compute_tile_order_packed")
 
 
 def compute_tile_order_packed_morton(tile_ranges_buf, total_tiles, x_blocks, tile_desc_buf, tile_order,
                                      tile_counts_buf, tile_ids_buf, sort_temp, zigzag_group_size,
                                      morton_bucket_size, /):
-    compute_tile_order_packed(tile_ranges_buf, total_tiles, x_blocks, tile_desc_buf, tile_order, tile_counts_buf,
-                              tile_ids_buf, sort_temp, zigzag_group_size)
+    """Order by (count bucket, Morton position) (render.cu:7050-7087)."""
+    if int(morton_bucket_size) <= 0:
+        raise GsrError(_lib.GSR_INVALID_ARG, "compute_tile_order_packed_morton: morton_bucket_size must be > 0")
+    _tile_order(tile_ranges_buf, total_tiles, x_blocks, morton_bucket_size, zigzag_group_size, tile_desc_buf,
+                tile_order, tile_counts_buf, tile_ids_buf, sort_temp, "compute_tile_order_packed_morton")
 
 
 # ---------------------------------------------------------------------------
