@@ -571,34 +571,49 @@ __global__ __launch_bounds__(kThreads, 3) void k_preprocess(const __grid_constan
 // farther out cannot pass it.
 constexpr int kMaxBandRows = 1024;  // tile rows of a CTA-swept rectangle that get candidate bands
 
-// Ellipse A dx^2 + 2B dx dy + C dy^2 <= w (w = 2 power) in float.  det = AC - B^2
-// is formed with a single rounding (Kahan's fused difference of products),
-// and the half-width at height dy as sqrt(det (dymax - dy)(dymax + dy)) / A,
-// which does not cancel near the top and bottom, so every extent carries a
-// few ulp of relative error: well under a pixel while the extents stay below
-// 1e6 px, against a margin of two tiles.  Ill-conditioned ellipses
-// (det <= 1e-6 AC), where the exact test itself is at the mercy of
-// cancellation, and non-finite values get every tile of the rectangle tested.
+// Ellipse A dx^2 + 2B dx dy + C dy^2 <= w (w = 2 power) in float.
+//
+// Which tiles can pass the exact test.  In exact arithmetic the test
+// (box_has_centre / box_hits_ellipse) only accepts tiles whose box meets the
+// ellipse.  In float it can also accept a tile just outside.  On a box edge
+// at offset dx from the centre, the test accepts a point of the edge where
+// the computed quadratic is <= 0; the computed discriminant errs by a few
+// 2^-24 of its terms' size, (B^2 + AC) dx^2 + C w, so every accepted point
+// satisfies Q <= w (1 + k u (1 + kappa)), with u = 2^-24, kappa = 2AC / det
+// >= (B^2 + AC) / det and k about 10 (the same holds for the horizontal
+// edge).  The candidate bands are therefore the exact row extents of the
+// ellipse inflated to w (1 + tau), tau = 64 u (1 + kappa), plus half a pixel
+// and a relative 1e-5 for the rounding of the band arithmetic itself and of
+// pixel coordinates.
+//
+// det = AC - B^2 is formed with a single rounding (Kahan's fused difference
+// of products), and the half-width at height dy as sqrt(det (dymax - dy)
+// (dymax + dy)) / A, which does not cancel near the top and bottom, so every
+// extent carries a few ulp of relative error.  Ill-conditioned ellipses
+// (det <= 1e-6 AC) and non-finite values get every tile of the rectangle
+// tested.
 struct Band {
     float B, inv_a, det, dymax, dxmax, dyr, cx, cy, m;
     bool ok;
 };
 
-__device__ __forceinline__ Band make_band(float3 q, float power, float2 c, float m)
+__device__ __forceinline__ Band make_band(float3 q, float power, float2 c)
 {
     Band b;
     const float A = q.x, B = q.y, C = q.z, w = 2.0f * power;
     const float bb = B * B;
     const float det = fmaf(A, C, -bb) + fmaf(-B, B, bb);
+    const float kappa = 2.0f * (A * C) / det;
+    const float wb = w * (1.0f + 64.0f * 5.9604645e-8f * (1.0f + kappa));  // inflated for the test's rounding
     b.B = B;
     b.inv_a = 1.0f / A;
     b.det = det;
-    b.dymax = sqrtf(w * A / det);
-    b.dxmax = sqrtf(w * C / det);
-    b.dyr = -B * sqrtf(w / (C * det));  // dy where the ellipse reaches its largest x
+    b.dymax = sqrtf(wb * A / det);
+    b.dxmax = sqrtf(wb * C / det);
+    b.dyr = -B * sqrtf(wb / (C * det));  // dy where the ellipse reaches its largest x
     b.cx = c.x;
     b.cy = c.y;
-    b.m = m;
+    b.m = 0.5f + 1e-5f * fmaxf(b.dxmax, b.dymax);
     b.ok = A > 0.0f && C > 0.0f && w > 0.0f && det > 1e-6f * (A * C) && b.dymax < 1e6f && b.dxmax < 1e6f &&
            fabsf(b.dyr) < 1e6f && fabsf(c.x) < 1e7f && fabsf(c.y) < 1e7f;
     return b;
@@ -638,7 +653,7 @@ __device__ __forceinline__ void sweep_cta(const MassiveEntry& me, const Preproce
     const int x_lo = me.rect.x & 0xFFFF, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
     const int w = x_hi - x_lo;
     // every thread forms the same band from the same inputs: a uniform branch
-    const Band eb = make_band(q, pw, c, 2.0f * (float)max(a.bx, a.by));
+    const Band eb = make_band(q, pw, c);
     if (eb.ok && (y_hi - y_lo) <= kMaxBandRows) {
         for (int r = threadIdx.x; r < y_hi - y_lo; r += kThreads) {
             int clo = 0, chi = -1;
@@ -693,7 +708,7 @@ __device__ __forceinline__ void sweep_warp(const MassiveEntry& me, const Preproc
     const float pw = me.ctr_power_depth.z;
     const float3 q = {me.conic_gid.x, me.conic_gid.y, me.conic_gid.z};
     const int x_lo = me.rect.x & 0xFFFF, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
-    const Band eb = make_band(q, pw, c, 2.0f * (float)max(a.bx, a.by));
+    const Band eb = make_band(q, pw, c);
     if (eb.ok) {
         for (int r0 = y_lo; r0 < y_hi; r0 += 32) {
             const int y = r0 + (int)lane;

@@ -139,6 +139,20 @@ def scene_clustered(n: int = 3_000_000, seed: int = 1) -> RawScene:
     return RawScene(means, log_scales, q, logits, shs)
 
 
+def scene_needles(n: int = 200_000, seed: int = 5) -> RawScene:
+    """Test scene of strongly anisotropic Gaussians: one axis up to e^7
+    (about 1100) times the other two, random orientations, many of them
+    large on screen.  Their conics are ill-conditioned, the hard case for the
+    tile tests."""
+    rng = _rng(seed)
+    means = rng.normal(0.0, 3.0, (n, 3)).astype(np.float32)
+    log_scales = np.empty((n, 3), np.float32)
+    log_scales[:, 0] = rng.uniform(-2.5, 0.0, n)
+    log_scales[:, 1:] = log_scales[:, :1] - rng.uniform(0.0, 7.0, (n, 2))
+    q, logits, shs = _common_attrs(rng, n)
+    return RawScene(means, log_scales, q, logits, shs)
+
+
 def scene_city(n: int = 20_000_000, seed: int = 2, n_clusters: int = 4096, per_cluster: int = 2000) -> RawScene:
     rng = _rng(seed)
     n_cl = min(n, n_clusters * per_cluster)

@@ -30,6 +30,8 @@ CASES = {
                                 lambda: scenes.camera_front(1280, 720, 1400.0 * 1280 / 1920)),
     "orbit_200k_1920x1080": (lambda: scenes.scene_clustered(200_000, seed=77),
                              lambda: scenes.orbit_camera(9.0, 2.1, -0.2, 1920, 1080, 1400.0)),
+    "needles_50k_1920x1080": (lambda: scenes.scene_needles(50_000, seed=5),
+                              lambda: scenes.orbit_camera(12.0, 0.4, 0.2, 1920, 1080, 1400.0)),
 }
 
 CAP = 8_000_000
