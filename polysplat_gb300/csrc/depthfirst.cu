@@ -305,7 +305,7 @@ cudaError_t launch_depth_first(const PreprocessParams& p0, bool half_sh, void* s
 
     // stable sort of the tile ids (M read on the device)
     const int tb = bits_for((uint32_t)tiles);
-    OrderMap ot{kOrderMasked, tb};
+    OrderMap ot{kOrderMasked, tb, 0};  // tile ids
     e = launch_sort32(0, p.counter, p.cap, ot, (tb + 7) / 8, tile_keys_in, vals_in, tile_keys_out, vals_out, tile_sort,
                       stream);
     if (e != cudaSuccess) return e;

@@ -247,7 +247,7 @@ gsr_status gsr_es_tile_sort(int num, int width, int height, int block_x, int blo
     SortScratch sc;
     if (!carve(sort_space, sort_bytes, num, sc)) return GSR_INVALID_ARG;
     const int bits = bits_for((uint32_t)(div_up(width, block_x) * div_up(height, block_y)));
-    const OrderMap order{kOrderMasked, bits};
+    const OrderMap order{kOrderMasked, bits, 0};  // tile ids
     cudaError_t e = launch_sort32(num, nullptr, num, order, (bits + 7) / 8, tile_keys_unsorted, values_unsorted,
                                   tile_keys_sorted, values_sorted, sc, s);
     if (e != cudaSuccess) return GSR_CUDA_ERROR;

@@ -176,6 +176,11 @@ enum : int {
 struct OrderMap {
     int kind;
     int end_bit;
+    // digits at or above this bit of the order word hold tile ids; where a key
+    // holds both depth and tile digits those passes rank with per-bit
+    // ballots, which beat match.any on them (kOrderDepthCompressed64 takes the
+    // boundary from the depth width on the device)
+    int tile_from_bit = 64;
 };
 struct SortScratch {
     WorkspaceHeader* hdr;  // counters, histograms, status, depth_hi

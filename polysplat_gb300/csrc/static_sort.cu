@@ -75,7 +75,7 @@ extern "C" gsr_status gsr_sort_bits_static(int num, const int32_t* d_num, int en
     e = cudaMemsetAsync(&hdr->status, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return GSR_CUDA_ERROR;
     const SortScratch sc = carve_sort_scratch(hdr, reinterpret_cast<char*>(base) + kHeaderBytes, kStaticSortKeys, 8);
-    const OrderMap order{kOrderMasked, end_bit};
+    const OrderMap order{kOrderMasked, end_bit, 32};  // tile << 32 | depth bits
     e = launch_sort64(num, d_num, capacity, order, (end_bit + 7) / 8, keys_in, values_in, keys_out, values_out, sc, s);
     return e == cudaSuccess ? GSR_OK : (e == cudaErrorInvalidValue ? GSR_INVALID_ARG : GSR_CUDA_ERROR);
 }
