@@ -132,9 +132,9 @@ constexpr size_t kMassiveQueueBytes = (size_t)kMassiveQueueEntries * sizeof(Mass
 // Small workspace for preprocess-only and render-only calls.
 constexpr size_t kSmallWorkspaceBytes = kHeaderBytes + kMassiveQueueBytes;
 
-constexpr int kSortThreads = 256;
+constexpr int kSortThreads = 512;
 constexpr int kSortItems = 8;
-constexpr int kSortTile = kSortThreads * kSortItems;  // 2048 keys per tile
+constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per tile
 constexpr int kMaxPasses = 8;
 
 size_t sort_workspace_bytes(long long cap);

@@ -190,8 +190,9 @@ struct PassSmem {
     int tile;
 };
 
-// Exclusive scan of 256 values held one per thread (blockDim == 256).
-__device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* warp_sums)
+// Exclusive scan of one value per thread over the whole CTA (kSortThreads);
+// the digit passes hold digit d's value in thread d and zeros above 255.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_sums)
 {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     uint32_t incl = v;
@@ -217,7 +218,7 @@ __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* war
 // 120 us and 125 vs 109 us on the two tile-bit passes); RANK 0 / 1 force
 // ballots / match.any.
 template <typename K, int RANK>
-__global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortJob<K> a, int pass)
+__global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortJob<K> a, int pass)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PassSmem<K>& S = *reinterpret_cast<PassSmem<K>*>(smem_raw);
@@ -249,7 +250,11 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortJob<K> a, int pass
     const bool clear_next = pass + 1 < passes;
     WorkspaceHeader* hdr = a.s.hdr;
 
-    S.gstart[threadIdx.x] = block_excl_scan256(hdr->hist[pass][threadIdx.x], S.warp_sums);
+    const bool digit_thread = threadIdx.x < 256;  // thread d owns digit d in the per-digit steps
+    {
+        const uint32_t g = block_excl_scan(digit_thread ? hdr->hist[pass][threadIdx.x] : 0u, S.warp_sums);
+        if (digit_thread) S.gstart[threadIdx.x] = g;
+    }
 
     for (;;) {
         if (threadIdx.x == 0) S.tile = (int)atomicAdd(&hdr->pass_counter[pass], 1u);
@@ -259,7 +264,7 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortJob<K> a, int pass
         if (tile >= tiles) break;
         const long long tbase = (long long)tile * kSortTile;
         const int tcount = (int)min((long long)kSortTile, (long long)n - tbase);
-        if (clear_next) look_next[(size_t)tile * 256 + threadIdx.x] = 0u;
+        if (clear_next && digit_thread) look_next[(size_t)tile * 256 + threadIdx.x] = 0u;
 
         // ---- load (warp-contiguous chunk) + stable per-warp rank ----
         K key[kSortItems];
@@ -313,22 +318,23 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_pass(SortJob<K> a, int pass
         __syncthreads();
 
         // ---- per-digit offsets: across warps, then across digits ----
-        uint32_t dtot;
+        uint32_t dtot = 0;
         {
             const int d = threadIdx.x;
-            uint32_t run = 0;
+            if (digit_thread) {
 #pragma unroll
-            for (int w = 0; w < kWarpsPerCta; w++) {
-                uint32_t c = S.whist[w][d];
-                S.whist[w][d] = run;
-                run += c;
+                for (int w = 0; w < kWarpsPerCta; w++) {
+                    uint32_t c = S.whist[w][d];
+                    S.whist[w][d] = dtot;
+                    dtot += c;
+                }
             }
-            dtot = run;
-            S.digit_excl[d] = block_excl_scan256(run, S.warp_sums);
+            const uint32_t ex = block_excl_scan(dtot, S.warp_sums);
+            if (digit_thread) S.digit_excl[d] = ex;
         }
 
         // ---- decoupled look-back: thread d owns digit d ----
-        {
+        if (digit_thread) {
             const int d = threadIdx.x;
             uint32_t* my = look + (size_t)tile * 256 + d;
             st_relaxed_u32(my, (tile == 0 ? kFlagPrefix : kFlagAgg) | dtot);
