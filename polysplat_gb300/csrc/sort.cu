@@ -10,7 +10,7 @@
 // Structure (one-sweep radix sort with decoupled look-back):
 //   1. k_upsweep: one read of all keys builds the 256-bin histogram of every
 //      8-bit digit pass at once, and clears the first look-back array.
-//   2. k_pass (one launch per digit): persistent CTAs take 2048-key tiles in
+//   2. k_pass (one launch per digit): persistent CTAs take 4096-key tiles in
 //      order from an atomic counter, rank keys stably inside the tile (per-warp
 //      ranking by match.any or by bit ballots), publish per-digit tile counts,
 //      look back over earlier tiles for the running per-digit prefix (bounded
