@@ -1007,6 +1007,15 @@ cudaError_t launch_scene_prepare(int P, const float* log_scales, const float* qu
     return cudaGetLastError();
 }
 
+// Persistent grid of the queue sweeps: as many CTAs as fit on every SM.
+template <typename Kern>
+static int emit_grid(Kern kern)
+{
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kThreads, 0) != cudaSuccess || b < 1) b = 4;
+    return device_sm_count() * b;
+}
+
 static cudaError_t preprocess_common(const PreprocessParams& p, bool half_sh, bool count, cudaStream_t stream)
 {
     if (p.P <= 0) return cudaSuccess;
@@ -1027,8 +1036,8 @@ static cudaError_t preprocess_common(const PreprocessParams& p, bool half_sh, bo
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.mq.capacity <= 0) return e;
     const DfEmit none{nullptr, nullptr, nullptr, nullptr, 0};
-    if (count) k_emit_massive<kMassiveCount, false><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, none);
-    else k_emit_massive<kMassiveEmit64, false><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, none);
+    if (count) k_emit_massive<kMassiveCount, false><<<emit_grid(k_emit_massive<kMassiveCount, false>), kThreads, 0, stream>>>(p, none);
+    else k_emit_massive<kMassiveEmit64, false><<<emit_grid(k_emit_massive<kMassiveEmit64, false>), kThreads, 0, stream>>>(p, none);
     return cudaGetLastError();
 }
 
@@ -1044,7 +1053,7 @@ cudaError_t launch_preprocess_views(const PreprocessParams& base, int n_views, i
     else k_preprocess<false, false, true><<<grid, kThreads, 0, stream>>>(base);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const DfEmit none{nullptr, nullptr, nullptr, nullptr, 0};
-    k_emit_massive<kMassiveEmit64, true><<<device_sm_count() * 4, kThreads, 0, stream>>>(base, none);
+    k_emit_massive<kMassiveEmit64, true><<<emit_grid(k_emit_massive<kMassiveEmit64, true>), kThreads, 0, stream>>>(base, none);
     return cudaGetLastError();
 }
 
@@ -1065,7 +1074,7 @@ cudaError_t launch_df_emit_massive(const PreprocessParams& p, const uint32_t* of
     // takes the queue again through the second pair of heads (cleared with
     // the rest of the preprocess region before the counting pass)
     const DfEmit df{offsets, rank, tiles, vals, cap};
-    k_emit_massive<kMassiveEmitDf, false><<<device_sm_count() * 4, kThreads, 0, stream>>>(p, df);
+    k_emit_massive<kMassiveEmitDf, false><<<emit_grid(k_emit_massive<kMassiveEmitDf, false>), kThreads, 0, stream>>>(p, df);
     return cudaGetLastError();
 }
 
