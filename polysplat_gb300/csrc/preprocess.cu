@@ -309,7 +309,7 @@ __device__ __forceinline__ void block_flush(Stage& st, const EmitOut& out, int* 
 // same tests, but each Gaussian's number of hit tiles is counted and written
 // with its depth and test geometry instead of keys.
 template <bool HALF, bool COUNT, bool VIEWS>
-__global__ __launch_bounds__(kThreads, 5) void k_preprocess(const __grid_constant__ PreprocessParams a0)
+__global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __grid_constant__ PreprocessParams a0)
 {
     // one view per grid row when VIEWS (parameter blocks in device memory)
     const PreprocessParams& a = VIEWS ? a0.views[blockIdx.y] : a0;
