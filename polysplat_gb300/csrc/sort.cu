@@ -114,9 +114,23 @@ __device__ __forceinline__ uint64_t order_word(uint32_t k, const KeyMap& m)
 
 __device__ __forceinline__ int passes_of(const KeyMap& m) { return (m.bits + 7) / 8; }
 
+// Eight consecutive keys from position b (a multiple of 8): 16-byte loads
+// for a full run of a 16-byte aligned buffer, single loads otherwise.
 template <typename K>
 __device__ __forceinline__ void load8(const K* src, long long b, int cnt, K (&k)[8])
 {
+    if (cnt == 8 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+        constexpr int kPer = 16 / sizeof(K);
+        const uint4* v = reinterpret_cast<const uint4*>(src + b);
+#pragma unroll
+        for (int q = 0; q < 8 / kPer; q++) {
+            const uint4 w = __ldg(v + q);
+            const K* e = reinterpret_cast<const K*>(&w);
+#pragma unroll
+            for (int j = 0; j < kPer; j++) k[q * kPer + j] = e[j];
+        }
+        return;
+    }
 #pragma unroll
     for (int j = 0; j < 8; j++) k[j] = j < cnt ? __ldg(src + b + j) : K(0);
 }
