@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--quick", action="store_true",
                     help="device-timed frames only (no e2e, CPU baseline or reference pipeline): for profiling")
     ap.add_argument("--cap-log2", type=int, default=0, help="key-buffer capacity 2^n (default: by scene size)")
+    ap.add_argument("--serve-profile", default=None, metavar="JSON",
+                    help="serve_mix only: skip the plain arm and the autotuner, serve the stream with this "
+                         "TuneConfig (JSON, e.g. the bench line's config.tuned) twice to warm up and once more "
+                         "inside the NVTX range 'timed', device-only: for ncu launch lists")
     ap.add_argument("--pipeline", default="single", choices=["single", "depth_first"],
                     help="single-pass 64-bit key sort, or depth sort + 32-bit tile sort")
     return ap.parse_args()
@@ -217,7 +221,9 @@ def run_gsr(args):
         dist.init_process_group("nccl", rank=rank, world_size=world)
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if args.workload == "serve_mix":
+    if args.workload == "serve_mix" and args.serve_profile:
+        line = run_serve_profile(args, dev)
+    elif args.workload == "serve_mix":
         line = run_serve(args, dev, rank, world, dist)
     elif args.workload == "diff_1m_8cam":
         line = run_diff(args, dev, rank, world, dist)
@@ -451,6 +457,28 @@ def forward_line(args, dev, rank, world, dist):
                         "d2h_bytes_per_step": cam.width * cam.height * 3 + 4},
                 "gpu_launches": launches_per_frame * K, "clocks": clocks}
     return line
+
+
+def run_serve_profile(args, dev):
+    """The served stream alone with a fixed configuration, for profiling."""
+    import torch
+
+    from polysplat_gb300 import Scene, scenes
+    from polysplat_gb300.serving import Server, TuneConfig
+
+    raws, reqs = scenes.serve_mix()
+    scs = [Scene.from_raw(r, dev) for r in raws]
+    cfg = TuneConfig(**json.loads(args.serve_profile))
+    srv = Server(scs, dev, 60 << 30, cfg)
+    for _ in range(2):
+        srv.run(reqs, realtime=False, deliver=False)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("timed")
+    st = srv.run(reqs, realtime=False, deliver=False)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    srv.close()
+    return {"workload": "serve_mix (profiling run)", "tuned": dataclasses.asdict(cfg), "served": st.as_dict()}
 
 
 def run_serve(args, dev, rank, world, dist):
