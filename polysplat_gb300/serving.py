@@ -54,6 +54,10 @@ class TuneConfig:
     massive_area: int = 32      # emission dispatch thresholds (tiles of a Gaussian's rectangle)
     huge_area: int = 2048
     variant: int = R.RENDER_PERSISTENT_FUSED
+    # tiles of all views of a small batch: the batch's sort key holds
+    # bits(tiles) tile bits above the depth bits, so a cap at a power of two
+    # can save a whole 8-bit digit pass per batch
+    max_batch_tiles: int = 1 << 30
 
 
 @dataclasses.dataclass
@@ -313,7 +317,8 @@ class Server:
             e = int(r.est * 1.25)
             t = ((r.cam.width + cfg.block_x - 1) // cfg.block_x) * ((r.cam.height + cfg.block_y - 1) // cfg.block_y)
             P = self.scenes[r.scene].num_vertex
-            if out and (keys + e > self.small_cap or g + P > self.max_g or tiles + t > self.tiles_cap):
+            if out and (keys + e > self.small_cap or g + P > self.max_g or tiles + t > self.tiles_cap
+                        or tiles + t > cfg.max_batch_tiles):
                 break
             out.append(r)
             keys, g, tiles = keys + e, g + P, tiles + t
@@ -421,7 +426,8 @@ class Server:
 DEFAULT_AXES = [(("block_x", "block_y"), [(32, 16), (32, 32)]),
                 ("large_keys", [2_000_000, 4_000_000, 16_000_000, 1 << 40]),
                 ("max_views", [4, 16]),
-                (("massive_area", "huge_area"), [(64, 4096), (16, 1024)])]
+                (("massive_area", "huge_area"), [(64, 4096), (16, 1024)]),
+                ("max_batch_tiles", [1 << 13, 1 << 14])]
 
 
 def autotune(scenes, sample_reqs, device, budget_bytes: int = 60 << 30, log=None, axes=None,
