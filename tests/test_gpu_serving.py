@@ -32,17 +32,21 @@ def _mix(n, rate_hz, seed=7):
     return raws, reqs
 
 
-def test_served_images_equal_alone(cuda_device):
+@pytest.mark.parametrize("tile", [(16, 16), (32, 32)])
+def test_served_images_equal_alone(cuda_device, tile):
+    """Both tile shapes the autotuner considers for the batched lane: each
+    request against the single-view forward with the same tile shape."""
+    bx, by = tile
     raws, reqs = _mix(40, 1000.0)
     scs = [Scene.from_raw(r, cuda_device) for r in raws]
-    cfg = TuneConfig(max_views=6, large_keys=400_000)  # both lanes take work
+    cfg = TuneConfig(max_views=6, large_keys=400_000, block_x=bx, block_y=by)  # both lanes take work
     srv = Server(scs, cuda_device, budget_bytes=6 << 30, config=cfg)
     st = srv.run(reqs, realtime=False)
     torch.cuda.synchronize()
     assert st.requests == len(reqs) and st.large > 0 and st.batches > 0 and st.mean_batch > 1.0
     alone = Rasterizer(max(scs, key=lambda s: s.num_vertex), 8_000_000, 1 << 16)
     for r in reqs:
-        img = alone.forward(scs[r.scene], Camera.from_spec(r.camera), torch.zeros(3),
+        img = alone.forward(scs[r.scene], Camera.from_spec(r.camera), torch.zeros(3), block_x=bx, block_y=by,
                             render_variant="preranges_smem_persistent_lite_e2e")
         s = image_stats(r.out.cpu().numpy(), img.cpu().numpy())
         assert s["max_abs"] <= 2 and s["psnr"] >= 50.0, (r.scene, r.camera.width, s)
