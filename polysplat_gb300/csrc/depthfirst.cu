@@ -9,8 +9,8 @@
 // idea, built on its own kernels:
 //   1. counting pass (preprocess.cu, COUNT mode): per Gaussian, the number of
 //      tiles its keys go to, its depth bits and its exact test geometry;
-//   2. k_df_compact: the emitting Gaussians, in index order (single-pass scan
-//      with decoupled look-back, deterministic);
+//   2. k_df_compact: the emitting Gaussians, in index order (reduce-then-scan,
+//      deterministic);
 //   3. depth sort of those V Gaussians (32-bit radix sort, sort.cu);
 //   4. k_df_offsets: where each Gaussian's pairs start, in depth order, and
 //      the total pair count M (written to the caller's key counter);
@@ -34,32 +34,6 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
-
-// Exclusive prefix of this tile's total over all earlier tiles (decoupled
-// look-back, one value per tile, bounded spin).  Called by thread 0.
-__device__ uint32_t tile_lookback(uint32_t* status, int tile, uint32_t total, uint32_t* err)
-{
-    st_relaxed_u32(status + tile, (tile == 0 ? kFlagPrefix : kFlagAgg) | (total & kValueMask));
-    uint32_t excl = 0;
-    int j = tile - 1;
-    uint32_t spins = 0;
-    while (j >= 0) {
-        const uint32_t v = ld_relaxed_u32(status + j);
-        if ((v & ~kValueMask) == 0u) {
-            if (++spins > kSpinLimit) {
-                record_error(err, kErrTimeout);
-                break;
-            }
-            __nanosleep(32);
-            continue;
-        }
-        excl += v & kValueMask;
-        if (v & kFlagPrefix) break;
-        j--;
-    }
-    if (tile != 0) st_relaxed_u32(status + tile, kFlagPrefix | ((excl + total) & kValueMask));
-    return excl;
-}
 
 // Block-wide exclusive scan of one value per thread; returns the total too.
 __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* s_warp, uint32_t& total)
@@ -94,24 +68,86 @@ struct DfArgs {
     const uint32_t* sgids;
     uint32_t* offsets;
     uint32_t* rank;
-    uint32_t* misc;         // [0] V, [1] compact tile counter, [2] offsets tile counter, [3] M
-    uint32_t* status_c;     // look-back of the compaction
-    uint32_t* status_o;     // look-back of the offsets scan
+    uint32_t* misc;         // [0] V, [3] M
+    uint32_t* sums_c;       // per-tile counts of emitting Gaussians, then their exclusive scan
+    uint32_t* sums_o;       // per-tile pair counts in depth order, then their exclusive scan
+    uint32_t* csorted;      // the pair counts in depth order
     int32_t* m_out;         // the caller's key counter
     uint32_t* err;          // workspace status word
 };
 
-// (2) the emitting Gaussians in index order with their depth bits
+// Both scans are reduce-then-scan: per-tile sums, one CTA scans the sums, and
+// each tile then scans itself from its base.  (A single pass with decoupled
+// look-back stalls here: with hundreds of CTAs in flight every tile walks
+// back over hundreds of unfinished predecessors.)
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* s_warp)
+{
+    uint32_t total;
+    block_scan(v, s_warp, total);
+    return total;
+}
+
+// (2a) per tile, how many Gaussians emit
+__global__ __launch_bounds__(kScanThreads) void k_df_compact_sums(const DfArgs a)
+{
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    const int ntiles = (a.P + kScanTile - 1) / kScanTile;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        uint32_t n = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            const int g = tile * kScanTile + k * kScanThreads + (int)threadIdx.x;
+            n += (g < a.P && __ldg(a.count + g) > 0u) ? 1u : 0u;
+        }
+        const uint32_t t = block_sum(n, s_warp);
+        if (threadIdx.x == 0) a.sums_c[tile] = t;
+    }
+}
+
+// (2b, 4b) exclusive scan of `n` tile sums in place by one CTA; the total goes
+// to misc[slot] (and, for the pair count, to the caller's key counter)
+__global__ __launch_bounds__(1024) void k_df_scan_sums(const uint32_t* d_n_elems, int n_max_elems, uint32_t* sums,
+                                                       uint32_t* misc, int slot, int32_t* m_out)
+{
+    __shared__ uint32_t s_w[32];
+    const int elems = d_n_elems ? (int)min(*d_n_elems, (uint32_t)n_max_elems) : n_max_elems;
+    const int nb = (elems + kScanTile - 1) / kScanTile;
+    const int per = (nb + 1023) / 1024, j0 = (int)threadIdx.x * per;
+    uint32_t v = 0;
+    for (int j = j0; j < min(nb, j0 + per); j++) v += sums[j];
+    uint32_t incl = v;
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(GSR_FULL_MASK, incl, d);
+        if (lane >= (unsigned)d) incl += t;
+    }
+    if (lane == 31) s_w[warp] = incl;
+    __syncthreads();
+    uint32_t wpre = 0, all = 0;
+    for (int w = 0; w < 32; w++) {
+        if (w < (int)warp) wpre += s_w[w];
+        all += s_w[w];
+    }
+    uint32_t run = wpre + incl - v;
+    for (int j = j0; j < min(nb, j0 + per); j++) {
+        const uint32_t c = sums[j];
+        sums[j] = run;
+        run += c;
+    }
+    if (threadIdx.x == 0) {
+        misc[slot] = all;
+        if (m_out) *m_out = (int32_t)all;
+    }
+}
+
+// (2c) the emitting Gaussians in index order with their depth bits
 __global__ __launch_bounds__(kScanThreads) void k_df_compact(const DfArgs a)
 {
     __shared__ uint32_t s_warp[kScanThreads / 32];
-    __shared__ uint32_t s_tile, s_base;
     const int ntiles = (a.P + kScanTile - 1) / kScanTile;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&a.misc[1], 1u);
-        __syncthreads();
-        const int tile = (int)s_tile;
-        if (tile >= ntiles) break;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int g0 = tile * kScanTile + threadIdx.x * kScanItems;  // 8 consecutive Gaussians per thread
         uint32_t flags = 0, n = 0;
 #pragma unroll
@@ -123,13 +159,7 @@ __global__ __launch_bounds__(kScanThreads) void k_df_compact(const DfArgs a)
             }
         }
         uint32_t total;
-        const uint32_t excl = block_scan(n, s_warp, total);
-        if (threadIdx.x == 0) {
-            s_base = tile_lookback(a.status_c, tile, total, a.err);
-            if (tile == ntiles - 1) a.misc[0] = s_base + total;
-        }
-        __syncthreads();
-        uint32_t pos = s_base + excl;
+        uint32_t pos = a.sums_c[tile] + block_scan(n, s_warp, total);
 #pragma unroll
         for (int j = 0; j < kScanItems; j++) {
             if (flags & (1u << j)) {
@@ -138,60 +168,59 @@ __global__ __launch_bounds__(kScanThreads) void k_df_compact(const DfArgs a)
                 pos++;
             }
         }
-        __syncthreads();
     }
 }
 
-// (4) offsets of each depth-ordered Gaussian's pairs; M = their total
+// (4a) the pair counts in depth order, and their per-tile sums
+__global__ __launch_bounds__(kScanThreads) void k_df_offsets_sums(const DfArgs a)
+{
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    const int V = (int)min(a.misc[0], (uint32_t)a.P);
+    const int ntiles = (V + kScanTile - 1) / kScanTile;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        uint32_t n = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            const int sidx = tile * kScanTile + k * kScanThreads + (int)threadIdx.x;
+            if (sidx < V) {
+                const uint32_t gid = __ldg(a.sgids + sidx);
+                const uint32_t c = gid < (uint32_t)a.P ? __ldg(a.count + gid) : 0u;
+                a.csorted[sidx] = c;
+                n += c;
+            }
+        }
+        const uint32_t t = block_sum(n, s_warp);
+        if (threadIdx.x == 0) a.sums_o[tile] = t;
+    }
+}
+
+// (4c) where each Gaussian's pairs start, in depth order, and its rank
 __global__ __launch_bounds__(kScanThreads) void k_df_offsets(const DfArgs a)
 {
     __shared__ uint32_t s_warp[kScanThreads / 32];
-    __shared__ uint32_t s_tile, s_base;
     const int V = (int)min(a.misc[0], (uint32_t)a.P);
     const int ntiles = (V + kScanTile - 1) / kScanTile;
-    if (V == 0) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            a.misc[3] = 0u;
-            *a.m_out = 0;
-        }
-        return;
-    }
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&a.misc[2], 1u);
-        __syncthreads();
-        const int tile = (int)s_tile;
-        if (tile >= ntiles) break;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int s0 = tile * kScanTile + threadIdx.x * kScanItems;
         uint32_t c[kScanItems];
         uint32_t n = 0;
 #pragma unroll
         for (int j = 0; j < kScanItems; j++) {
-            const int s = s0 + j;
-            c[j] = s < V ? __ldg(a.count + __ldg(a.sgids + s)) : 0u;
+            c[j] = s0 + j < V ? __ldg(a.csorted + s0 + j) : 0u;
             n += c[j];
         }
         uint32_t total;
-        const uint32_t excl = block_scan(n, s_warp, total);
-        if (threadIdx.x == 0) {
-            s_base = tile_lookback(a.status_o, tile, total, a.err);
-            if (tile == ntiles - 1) {
-                const uint32_t m = s_base + total;
-                a.misc[3] = m;
-                *a.m_out = (int32_t)m;
-            }
-        }
-        __syncthreads();
-        uint32_t off = s_base + excl;
+        uint32_t off = a.sums_o[tile] + block_scan(n, s_warp, total);
 #pragma unroll
         for (int j = 0; j < kScanItems; j++) {
-            const int s = s0 + j;
-            if (s < V) {
-                a.offsets[s] = off;
-                a.rank[__ldg(a.sgids + s)] = (uint32_t)s;
+            const int sidx = s0 + j;
+            if (sidx < V) {
+                a.offsets[sidx] = off;
+                const uint32_t gid = __ldg(a.sgids + sidx);
+                if (gid < (uint32_t)a.P) a.rank[gid] = (uint32_t)sidx;
                 off += c[j];
             }
         }
-        __syncthreads();
     }
 }
 
@@ -210,11 +239,10 @@ size_t df_scratch_bytes(int P)
 }
 
 struct DfLayout {
-    uint32_t *misc, *count, *dkey, *rank, *ckeys, *cgids, *skeys, *sgids, *offsets, *status_c, *status_o;
+    uint32_t *misc, *count, *dkey, *rank, *ckeys, *cgids, *skeys, *sgids, *offsets, *sums_c, *sums_o;
     float4* geo;
     int2* rect;
     void* sort_mem;
-    size_t status_bytes;
 };
 
 static DfLayout df_layout(void* scratch, int P)
@@ -235,10 +263,9 @@ static DfLayout df_layout(void* scratch, int P)
     o += al(p * 16);
     L.rect = reinterpret_cast<int2*>(b + o);
     o += al(p * 8);
-    L.status_c = reinterpret_cast<uint32_t*>(b + o);
-    L.status_o = reinterpret_cast<uint32_t*>(b + o + al(tiles * 4));
-    L.status_bytes = 2 * al(tiles * 4);
-    o += L.status_bytes;
+    L.sums_c = reinterpret_cast<uint32_t*>(b + o);
+    L.sums_o = reinterpret_cast<uint32_t*>(b + o + al(tiles * 4));
+    o += 2 * al(tiles * 4);
     L.sort_mem = b + o;
     return L;
 }
@@ -260,9 +287,7 @@ cudaError_t launch_depth_first(const PreprocessParams& p0, bool half_sh, void* s
     if (e != cudaSuccess) return e;
     profile_mark(stream);
 
-    // clear the scan counters / look-back state (misc + both status arrays)
     if ((e = cudaMemsetAsync(L.misc, 0, 256, stream)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(L.status_c, 0, L.status_bytes, stream)) != cudaSuccess) return e;
     if (p.P > 0) {
         DfArgs a;
         a.P = p.P;
@@ -274,13 +299,16 @@ cudaError_t launch_depth_first(const PreprocessParams& p0, bool half_sh, void* s
         a.offsets = L.offsets;
         a.rank = L.rank;
         a.misc = L.misc;
-        a.status_c = L.status_c;
-        a.status_o = L.status_o;
+        a.sums_c = L.sums_c;
+        a.sums_o = L.sums_o;
+        a.csorted = L.skeys;  // the sorted depth keys are not read after the depth sort
         a.m_out = p.counter;
         a.err = &hdr->status;
         const int sms = device_sm_count();
-        const int ntiles = div_up(p.P, kScanTile);
-        k_df_compact<<<std::min(ntiles, sms * 4), kScanThreads, 0, stream>>>(a);
+        const int grid = std::min(div_up(p.P, kScanTile), sms * 8);
+        k_df_compact_sums<<<grid, kScanThreads, 0, stream>>>(a);
+        k_df_scan_sums<<<1, 1024, 0, stream>>>(nullptr, p.P, L.sums_c, L.misc, 0, nullptr);
+        k_df_compact<<<grid, kScanThreads, 0, stream>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         profile_mark(stream);
 
@@ -291,7 +319,9 @@ cudaError_t launch_depth_first(const PreprocessParams& p0, bool half_sh, void* s
                           L.sgids, ds, stream);
         if (e != cudaSuccess) return e;
 
-        k_df_offsets<<<std::min(ntiles, sms * 4), kScanThreads, 0, stream>>>(a);
+        k_df_offsets_sums<<<grid, kScanThreads, 0, stream>>>(a);
+        k_df_scan_sums<<<1, 1024, 0, stream>>>(&L.misc[0], p.P, L.sums_o, L.misc, 3, p.counter);
+        k_df_offsets<<<grid, kScanThreads, 0, stream>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         profile_mark(stream);
         e = launch_df_emit_small(p, &L.misc[0], L.sgids, L.offsets, tile_keys_in, vals_in, p.cap, stream);
