@@ -349,7 +349,7 @@ def forward_line(args, dev, rank, world, dist):
     working = [t for t in pass_ms if t > 0.2 * max(pass_ms)]
     pass_avg = statistics.mean(working)
 
-    # algorithmic bytes per launch (formulas in the design doc)
+    # algorithmic bytes per launch: every byte the kernel must move once
     P = scene.num_vertex
     peak, peak_kind = measured_peaks()
     # a digit pass reads and writes every (key, value) pair: 12-byte pairs in
