@@ -12,7 +12,7 @@
 // The per-view parameter blocks live in device memory: they are packed on
 // the host into a pinned staging slot and copied to the device ahead of the
 // kernels.  The kernel sequence depends only on the batch's shape (views,
-// rows of preprocess blocks, total tiles, tile shape, variant), so it is
+// preprocess blocks over all views, total tiles, tile shape, variant), so it is
 // captured once per shape into a CUDA graph and replayed for any cameras,
 // scenes of the same size class and output buffers.
 #include <cstring>
@@ -29,13 +29,17 @@ namespace {
 constexpr int kStagingSlots = 4;
 
 struct Shape {
-    int variant, half, bx, by, n_views, rows, tiles;
+    int variant, half, bx, by, n_views, blocks, tiles;
     bool operator<(const Shape& o) const
     {
-        return std::tie(variant, half, bx, by, n_views, rows, tiles) <
-               std::tie(o.variant, o.half, o.bx, o.by, o.n_views, o.rows, o.tiles);
+        return std::tie(variant, half, bx, by, n_views, blocks, tiles) <
+               std::tie(o.variant, o.half, o.bx, o.by, o.n_views, o.blocks, o.tiles);
     }
 };
+
+// Preprocess blocks of a batch, rounded up so that batches of similar size
+// share a captured graph (the extra blocks return at once).
+constexpr int kBlockBucket = 512;
 
 }  // namespace
 }  // namespace gsr
@@ -147,7 +151,7 @@ void pack_view(PreprocessParams& p, const gsr_scene_ref& sc, const gsr_view& v, 
 }
 
 // The kernel sequence of a batch (everything after the parameter copy).
-cudaError_t enqueue(gsr_batcher* b, const Shape& s, int max_P, cudaStream_t st)
+cudaError_t enqueue(gsr_batcher* b, const Shape& s, cudaStream_t st)
 {
     WorkspaceHeader* h = reinterpret_cast<WorkspaceHeader*>(b->ws);
     cudaError_t e = cudaMemsetAsync(&h->status, 0, sizeof(uint32_t), st);
@@ -169,7 +173,7 @@ cudaError_t enqueue(gsr_batcher* b, const Shape& s, int max_P, cudaStream_t st)
     base.n_views = s.n_views;
     base.bx = s.bx;
     base.by = s.by;
-    e = launch_preprocess_views(base, s.n_views, max_P, s.half != 0, st);
+    e = launch_preprocess_views(base, s.n_views, s.blocks, s.half != 0, st);
     if (e != cudaSuccess) return e;
     SortArgs sa;
     sa.num = 0;
@@ -289,7 +293,7 @@ gsr_status gsr_batcher_render(gsr_batcher* b, int variant, int shs_half, int blo
     std::lock_guard<std::mutex> lk(b->mu);
     // layout of the batch: first feature slot and first tile of every view
     long long g = 0;
-    int tiles = 0, max_P = 0;
+    int tiles = 0, blocks = 0;
     for (int i = 0; i < n_views; i++) {
         const gsr_view& v = views[i];
         if (v.scene < 0 || v.scene >= n_scenes || v.width <= 0 || v.height <= 0 || !v.out) return GSR_INVALID_ARG;
@@ -298,7 +302,7 @@ gsr_status gsr_batcher_render(gsr_batcher* b, int variant, int shs_half, int blo
         if (div_up(v.width, block_x) >= 65536) return GSR_INVALID_ARG;
         g += sc.P;
         tiles += div_up(v.width, block_x) * div_up(v.height, block_y);
-        if (sc.P > max_P) max_P = sc.P;
+        blocks += div_up(sc.P, 256);
         if (g > b->max_gaussians || tiles > b->max_tiles) return GSR_INVALID_ARG;
     }
     // pack the parameter blocks into a free staging slot
@@ -334,10 +338,10 @@ gsr_status gsr_batcher_render(gsr_batcher* b, int variant, int shs_half, int blo
     if (e != cudaSuccess) return GSR_CUDA_ERROR;
     b->last_total = tiles;
 
-    const Shape s{variant, shs_half ? 1 : 0, block_x, block_y, n_views, div_up(max_P > 0 ? max_P : 1, 256), tiles};
-    const int rows_P = s.rows * 256;  // preprocess grid covers the largest scene of this shape
+    const Shape s{variant, shs_half ? 1 : 0, block_x, block_y, n_views,
+                  div_up(blocks > 0 ? blocks : 1, kBlockBucket) * kBlockBucket, tiles};
     if (!use_graph || st == nullptr) {
-        e = enqueue(b, s, rows_P, st);
+        e = enqueue(b, s, st);
         return e == cudaSuccess ? GSR_OK : GSR_CUDA_ERROR;
     }
     auto it = b->graphs.find(s);
@@ -346,12 +350,12 @@ gsr_status gsr_batcher_render(gsr_batcher* b, int variant, int shs_half, int blo
         // and occupancy queries happen outside any capture); the second is
         // captured and every later one replays the graph
         if (b->seen[s]++ == 0) {
-            e = enqueue(b, s, rows_P, st);
+            e = enqueue(b, s, st);
             return e == cudaSuccess ? GSR_OK : GSR_CUDA_ERROR;
         }
         cudaGraph_t graph = nullptr;
         if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return GSR_CUDA_ERROR;
-        const cudaError_t ce = enqueue(b, s, rows_P, st);
+        const cudaError_t ce = enqueue(b, s, st);
         const cudaError_t ee = cudaStreamEndCapture(st, &graph);
         if (ce != cudaSuccess || ee != cudaSuccess || !graph) {
             if (graph) cudaGraphDestroy(graph);

@@ -80,7 +80,9 @@ cudaError_t launch_preprocess(const PreprocessParams& p, bool half_sh, cudaStrea
 // One preprocess (+ large-Gaussian emission) over n_views views whose
 // parameter blocks are in device memory at base.views (shared fields --
 // queue, keys, counter -- are the same in every block and in `base`).
-cudaError_t launch_preprocess_views(const PreprocessParams& base, int n_views, int max_P, bool half_sh,
+// `blocks` covers the views' Gaussians one view after another (at least
+// sum over views of ceil(P / 256)); blocks past the last view return at once.
+cudaError_t launch_preprocess_views(const PreprocessParams& base, int n_views, int blocks, bool half_sh,
                                     cudaStream_t stream);
 // Depth-first pipeline: counting pass (fills p.df, features and the massive
 // queue), then the emission of a Gaussian's pairs at its offset (small

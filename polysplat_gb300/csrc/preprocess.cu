@@ -311,9 +311,24 @@ __device__ __forceinline__ void block_flush(Stage& st, const EmitOut& out, int* 
 template <bool HALF, bool COUNT, bool VIEWS>
 __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __grid_constant__ PreprocessParams a0)
 {
-    // one view per grid row when VIEWS (parameter blocks in device memory)
-    const PreprocessParams& a = VIEWS ? a0.views[blockIdx.y] : a0;
-    const uint32_t view_tag = VIEWS ? (blockIdx.y << 16) : 0u;
+    // VIEWS: the views' blocks follow one another along the grid (parameter
+    // blocks in device memory); a block past the last view has no work
+    int vi = 0, lblock = (int)blockIdx.x;
+    if (VIEWS) {
+        vi = -1;
+        for (int u = 0, start = 0; u < a0.n_views; u++) {
+            const int nb = (a0.views[u].P + kThreads - 1) / kThreads;
+            if (lblock < start + nb) {
+                vi = u;
+                lblock -= start;
+                break;
+            }
+            start += nb;
+        }
+        if (vi < 0) return;
+    }
+    const PreprocessParams& a = VIEWS ? a0.views[vi] : a0;
+    const uint32_t view_tag = VIEWS ? ((uint32_t)vi << 16) : 0u;
     __shared__ uint64_t s_keys[COUNT ? 1 : kWarps][kStage];
     __shared__ uint32_t s_vals[COUNT ? 1 : kWarps][kStage];
     __shared__ int s_fill[kWarps];
@@ -324,7 +339,7 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
 
     const unsigned lane = threadIdx.x & 31u;
     const int warp = threadIdx.x >> 5;
-    const int idx = blockIdx.x * kThreads + threadIdx.x;
+    const int idx = lblock * kThreads + threadIdx.x;
     const int warp_first = idx - (int)lane;
     const int tx = lane & 7, ty = lane >> 3;  // 8x4 tile window of the massive path
     const int gridx = a.gx, gridy = a.gy;
@@ -1041,14 +1056,14 @@ static cudaError_t preprocess_common(const PreprocessParams& p, bool half_sh, bo
     return cudaGetLastError();
 }
 
-cudaError_t launch_preprocess_views(const PreprocessParams& base, int n_views, int max_P, bool half_sh,
+cudaError_t launch_preprocess_views(const PreprocessParams& base, int n_views, int blocks, bool half_sh,
                                     cudaStream_t stream)
 {
-    if (n_views <= 0 || max_P <= 0) return cudaSuccess;
+    if (n_views <= 0 || blocks <= 0) return cudaSuccess;
     if (n_views > 32767 || !base.views || base.mq.capacity <= 0) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(base.mq.count, 0, kPreprocessRegionBytes, stream);
     if (e != cudaSuccess) return e;
-    const dim3 grid(div_up(max_P, kThreads), n_views);
+    const dim3 grid(blocks);
     if (half_sh) k_preprocess<true, false, true><<<grid, kThreads, 0, stream>>>(base);
     else k_preprocess<false, false, true><<<grid, kThreads, 0, stream>>>(base);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
