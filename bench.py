@@ -69,6 +69,18 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest of every rank's value (timings are reported for the slowest
+    replica); the value itself on one process."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ----------------------------------------------------------------------------- clocks
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -327,10 +339,7 @@ def forward_line(args, dev, rank, world, dist):
         dist.barrier()
     clocks = sampler.stop()
     elapsed_ms = t_start.elapsed_time(t_end)
-    if dist is not None:
-        t = torch.tensor([elapsed_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, dist, dev)
     fps = world * K / (elapsed_ms / 1000.0)
 
     if df:
@@ -549,10 +558,7 @@ def run_serve(args, dev, rank, world, dist):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = serve_cpu_baseline(raws, reqs, seconds=15.0)
     wall = s_sat.wall_s
-    if dist is not None:
-        t = torch.tensor([wall], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        wall = float(t.item())
+    wall = max_over_ranks(wall, dist, dev)
     value = world * len(reqs) / wall
     img_bytes = sum(r.camera.width * r.camera.height * 3 for r in reqs) / len(reqs)
     # kernel launches of the saturated run: small batches (preprocess, large-
@@ -632,10 +638,7 @@ def run_diff(args, dev, rank, world, dist):
     torch.cuda.synchronize()
     clocks = sampler.stop()
     ms = a.elapsed_time(b) / K
-    if dist is not None:
-        tt = torch.tensor([ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(ms, dist, dev)
     if rank != 0:
         return None
     views = world * len(cams) * 1000.0 / ms
