@@ -425,7 +425,7 @@ class Server:
 # ----------------------------------------------------------------------------- autotuner
 DEFAULT_AXES = [(("block_x", "block_y"), [(32, 16), (32, 32)]),
                 ("large_keys", [2_000_000, 4_000_000, 16_000_000, 1 << 40]),
-                ("max_views", [4, 16]),
+                ("max_views", [4, 8, 16]),
                 (("massive_area", "huge_area"), [(64, 4096), (16, 1024)]),
                 ("max_batch_tiles", [1 << 13, 1 << 14])]
 
