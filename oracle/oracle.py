@@ -13,8 +13,6 @@ from __future__ import annotations
 import ctypes
 import os
 import subprocess
-import sys
-from typing import Optional
 
 import numpy as np
 

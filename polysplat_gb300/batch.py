@@ -8,7 +8,7 @@ only packs the per-view descriptors.
 from __future__ import annotations
 
 import ctypes
-from typing import List, Optional, Sequence
+from typing import Optional, Sequence
 
 import torch
 

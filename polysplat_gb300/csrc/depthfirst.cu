@@ -31,9 +31,6 @@ namespace {
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
-constexpr uint32_t kFlagAgg = 1u << 30;
-constexpr uint32_t kFlagPrefix = 2u << 30;
-constexpr uint32_t kValueMask = (1u << 30) - 1u;
 
 // Block-wide exclusive scan of one value per thread; returns the total too.
 __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* s_warp, uint32_t& total)

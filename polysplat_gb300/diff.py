@@ -19,7 +19,7 @@ from typing import Sequence
 import torch
 
 from . import _lib as R
-from ._lib import GsrError, check, lib
+from ._lib import check, lib
 from .ops import get_sort_buffer_size
 from .rasterizer import Camera
 

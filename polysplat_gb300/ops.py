@@ -23,7 +23,6 @@ Differences a caller can observe, all deliberate:
 from __future__ import annotations
 
 import ctypes
-import struct
 from typing import Dict, Tuple
 
 import numpy as np

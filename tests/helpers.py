@@ -3,8 +3,6 @@ import math
 
 import numpy as np
 
-from oracle import oracle as O
-
 
 def psnr(a: np.ndarray, b: np.ndarray) -> float:
     d = a.astype(np.float64) - b.astype(np.float64)
@@ -35,22 +33,6 @@ def compare_key_lists(gk, gv, ok, ov):
     only_o = op.size - common.size
     ulp = int(np.abs(gd[gi] - od[oi]).max()) if common.size else 0
     return only_g, only_o, ulp
-
-
-def values_equal_within_key_runs(keys, vals_a, vals_b):
-    """Values agree except for order inside runs of equal keys."""
-    if keys.size == 0:
-        return True
-    brk = np.flatnonzero(np.diff(keys.astype(np.uint64)) != 0) + 1
-    starts = np.concatenate([[0], brk])
-    ends = np.concatenate([brk, [keys.size]])
-    for s, e in zip(starts, ends):
-        if e - s == 1:
-            if vals_a[s] != vals_b[s]:
-                return False
-        elif not np.array_equal(np.sort(vals_a[s:e]), np.sort(vals_b[s:e])):
-            return False
-    return True
 
 
 def random_tile_keys(rng, n, tiles, dup_frac=0.2, high_garbage=False, end_bit=64):

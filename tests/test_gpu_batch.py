@@ -7,7 +7,6 @@ exact); every image within max-abs 2/255 and PSNR >= 50 dB of its
 single-view render (keys of equal tile and depth may blend in another
 order); the graph replay with new cameras matches fresh single-view renders.
 """
-import numpy as np
 import pytest
 import torch
 

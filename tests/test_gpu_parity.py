@@ -8,7 +8,6 @@ floating-point stages the tolerances are written beside each assert:
     rel 2e-4 (fast-math lg2/rsqrt/sqrt vs exact FP64);
   * images: max-abs <= 2/255 and PSNR >= 50 dB.
 """
-import ctypes
 
 import numpy as np
 import pytest
@@ -18,7 +17,7 @@ from oracle import oracle as O
 from polysplat_gb300 import Camera, Rasterizer, Scene, ops, scenes
 from polysplat_gb300._lib import GsrError, lib
 
-from helpers import (compare_key_lists, image_stats, random_tile_keys, values_equal_within_key_runs)
+from helpers import compare_key_lists, image_stats, random_tile_keys
 
 pytestmark = pytest.mark.gpu
 

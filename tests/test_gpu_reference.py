@@ -19,7 +19,7 @@ from oracle import oracle as O
 from oracle import refkernels as RK
 from polysplat_gb300 import Camera, Scene, ops, scenes
 
-from helpers import compare_key_lists, image_stats, values_equal_within_key_runs
+from helpers import compare_key_lists, image_stats
 
 pytestmark = [pytest.mark.gpu,
               pytest.mark.skipif(not RK.available(), reason="reference device images not built")]

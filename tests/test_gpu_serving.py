@@ -2,7 +2,6 @@
 equals its image rendered alone (within max-abs 2/255 and PSNR >= 50 dB),
 through both lanes; the real-time replay completes every request; the
 autotuner returns a configuration that serves."""
-import dataclasses
 
 import numpy as np
 import pytest
