@@ -319,13 +319,13 @@ gsr_status gsr_batcher_finish(gsr_batcher* b, int32_t* num_rendered, gsr_stream_
 /* Graphs captured so far; device addresses of the batch's key counter and
  * status word (for asynchronous read-back). */
 int gsr_batcher_graphs(const gsr_batcher* b);
+const int32_t* gsr_batcher_counter(const gsr_batcher* b);
+const uint32_t* gsr_batcher_status(const gsr_batcher* b);
 /* Dispatch thresholds of the tile-key emission, in tiles of a Gaussian's
  * rectangle: from massive_area (default 32) on, a rectangle is queued for the
  * large-Gaussian kernel; from huge_area (default 2048) on, a whole CTA sweeps
  * it.  They change which scheme tests the tiles, never the keys. */
 gsr_status gsr_batcher_set_thresholds(gsr_batcher* b, int massive_area, int huge_area);
-const int32_t* gsr_batcher_counter(const gsr_batcher* b);
-const uint32_t* gsr_batcher_status(const gsr_batcher* b);
 
 /* ---- stage timing ------------------------------------------------------- */
 /* Profiling hook with no counterpart in the reference.  After
