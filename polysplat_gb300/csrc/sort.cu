@@ -8,14 +8,16 @@
 // so no host synchronisation is needed between the producer and the sort.
 //
 // Structure (one-sweep radix sort with decoupled look-back):
-//   1. k_upsweep: one read of all keys builds the 256-bin histogram of every
-//      8-bit digit pass at once, and clears the first look-back array.
+//   1. k_upsweep: one read of all keys builds the 256-bin histogram of the
+//      first 8-bit digit, and clears the first look-back array.
 //   2. k_pass (one launch per digit): persistent CTAs take 4096-key tiles in
 //      order from an atomic counter, rank keys stably inside the tile (per-warp
 //      ranking by match.any or by bit ballots), publish per-digit tile counts,
 //      look back over earlier tiles for the running per-digit prefix (bounded
 //      spin, four predecessors per round trip), reorder the tile in shared
-//      memory by digit and write it out with coalesced stores.
+//      memory by digit and write it out with coalesced stores.  While it holds
+//      a tile's keys it also counts their next digit, so the next pass's
+//      histogram is complete when this launch ends.
 //
 // Keys are mapped to an "ordering word" before digits are taken (OrderMap):
 // the masked key, or -- for keys the preprocess emitted -- the depth bits
