@@ -2,21 +2,31 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl gsr|reference]
 
-A step is one frame of the plain forward (preprocess -> tile-key radix sort
--> tile ranges -> persistent blend) over a resident seeded synthetic scene.
-Default workload: ``plain_3m_1080p`` (3,000,000 Gaussians, clustered with a
-heavy-tailed scale distribution, 1920x1080, fx=fy=1400, 16x16 tiles, FP16
-SH -- the reference's E2E variant ``preranges_smem_persistent_lite_e2e``).
+Default workload: ``serve_mix``, a stream of 512 render requests (Poisson
+arrivals at 240/s) over resident scenes of 0.5, 2, 5 and 10 M Gaussians at
+720p-2160p, served by continuous batching against the plain per-request
+forward; a step is one request, and the line also carries a config-1 plain
+forward measurement.
+
+Plain-forward workloads (``plain_3m_1080p``: 3,000,000 Gaussians, clustered
+with a heavy-tailed scale distribution, 1920x1080, fx=fy=1400, 16x16 tiles,
+FP16 SH, the reference's E2E variant ``preranges_smem_persistent_lite_e2e``;
+also ``city_20m_8k``, ``clustered_1m_1080p``, ``plain_100k_800x600``): a step
+is one frame (preprocess -> tile-key radix sort -> tile ranges -> persistent
+blend).
 
 value     frames/s, device-timed over K back-to-back frames (CUDA events on
-          the launching stream; inputs resident in HBM; the scene, 408 MB,
-          is larger than L2, so no flush is needed between frames).
+          the launching stream; inputs resident in HBM; the scenes are larger
+          than L2, so no flush is needed between frames).
 e2e       frames/s through the public drop-in API (Rasterizer.forward with
           the host-read camera/background, status read-back and the frame
           copied to pinned host memory every step).
 roofline  the dominant kernel of the frame, timed live with CUDA events
           recorded between stages on the launching stream.
 cpu_baseline  the FP64 CPU oracle (oracle/), multithreaded, on whole frames.
+
+``gather_plain_3m_1080p`` times the feature gather (gather_features) alone,
+over the sorted list of one plain_3m_1080p frame: GB/s of algorithmic bytes.
 
 --impl reference runs the reference's CPU arm: the reference ships no CPU
 path, so this is the FP64 oracle restatement of its algorithm on all host
@@ -47,7 +57,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", default="serve_mix",
                     help="serve_mix (config 3, the headline), or a plain-forward workload: plain_3m_1080p, "
-                         "plain_100k_800x600, clustered_1m_1080p, city_20m_8k")
+                         "plain_100k_800x600, clustered_1m_1080p, city_20m_8k; diff_1m_8cam (forward + "
+                         "backward); gather_plain_3m_1080p (the feature gather alone)")
     ap.add_argument("--impl", default="gsr", choices=["gsr", "reference", "reference-gpu"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true",
@@ -239,6 +250,8 @@ def run_gsr(args):
         line = run_serve(args, dev, rank, world, dist)
     elif args.workload == "diff_1m_8cam":
         line = run_diff(args, dev, rank, world, dist)
+    elif args.workload == "gather_plain_3m_1080p":
+        line = run_gather(args, dev, rank, world, dist)
     else:
         line = forward_line(args, dev, rank, world, dist)
     if rank == 0 and line is not None:
@@ -589,6 +602,63 @@ def run_serve(args, dev, rank, world, dist):
             if fwd else None,
             "cpu_baseline": cpu,
             "gpu_launches": launches, "clocks": clocks}
+
+
+def run_gather(args, dev, rank, world, dist):
+    """The feature gather (gather_features; the reference's gather.cu:6-22)
+    alone, over the sorted values of one plain_3m_1080p frame: per key, the
+    4-byte index, a random read of the Gaussian's 40 bytes of features
+    (xy, rgb + depth, conic + log2 opacity) and a sequential 40-byte write.
+    `value` is GB/s of those algorithmic bytes, CUDA-event timed; the 9.2 M
+    keys move 773 MB per step, larger than L2."""
+    import torch
+
+    from polysplat_gb300 import Camera, Rasterizer, Scene, ops, scenes
+
+    raw, cams = scenes.workload("plain_3m_1080p")
+    scene = Scene.from_raw(raw, dev)
+    cam = Camera.from_spec(cams[0])
+    cap = 1 << 26
+    rast = Rasterizer(scene, cap, 1 << 18)
+    rast.forward(scene, cam, torch.zeros(3), render_variant="preranges_smem_persistent_lite_e2e", use_es=False)
+    torch.cuda.synchronize()
+    M = int(rast.curr_offset.item())
+    vals = rast.gaussian_values_sorted[:M]
+    dst = [torch.empty((M, k), device=dev, dtype=torch.float32) for k in (2, 4, 4)]
+    src = (rast.points_xy, rast.rgb_depth, rast.conic_opacity)
+    per_key = 4 + 2 * sum(t.shape[1] * 4 for t in dst)
+    for _ in range(max(3, args.warmup)):
+        ops.gather_features(M, vals, *src, *dst)
+    K = max(3, args.steps)
+    sampler = ClockSampler(dev.index or 0)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)
+    stream = torch.cuda.current_stream(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(K):
+        ops.gather_features(M, vals, *src, *dst)
+    b.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = max_over_ranks(a.elapsed_time(b) / K, dist, dev)
+    if rank != 0:
+        return None
+    gbs = world * M * per_key / (ms * 1e-3) / 1e9
+    peak = measured_peaks()
+    return {"metric": "GB/s", "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "gather_plain_3m_1080p", "keys": M, "bytes_per_key": per_key,
+                       "l2": "%.0f MB per step, larger than L2; the %.0f MB feature table it reads at random can "
+                             "stay in L2" % (M * per_key / 1e6, sum(t.numel() * 4 for t in src) / 1e6),
+                       "parallelism": "single"},
+            "roofline": {"bound": "hbm", "kernel": "k_gather", "achieved": gbs / world, "peak": peak[0],
+                         "unit": "GB/s", "frac": gbs / world / peak[0], "peak_kind": peak[1], "traffic": None},
+            "gpu_launches": K, "clocks": clocks}
 
 
 def run_diff(args, dev, rank, world, dist):
