@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--workload", default="serve_mix",
                     help="serve_mix (config 3, the headline), or a plain-forward workload: plain_3m_1080p, "
                          "plain_100k_800x600, clustered_1m_1080p, city_20m_8k; diff_1m_8cam (forward + "
-                         "backward); gather_plain_3m_1080p (the feature gather alone)")
+                         "backward); gather_plain_3m_1080p, prepare_plain_3m (the feature gather or the scene "
+                         "transform alone)")
     ap.add_argument("--impl", default="gsr", choices=["gsr", "reference", "reference-gpu"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true",
@@ -252,6 +253,8 @@ def run_gsr(args):
         line = run_diff(args, dev, rank, world, dist)
     elif args.workload == "gather_plain_3m_1080p":
         line = run_gather(args, dev, rank, world, dist)
+    elif args.workload == "prepare_plain_3m":
+        line = run_prepare(args, dev, rank, world, dist)
     else:
         line = forward_line(args, dev, rank, world, dist)
     if rank == 0 and line is not None:
@@ -657,6 +660,72 @@ def run_gather(args, dev, rank, world, dist):
                              "stay in L2" % (M * per_key / 1e6, sum(t.numel() * 4 for t in src) / 1e6),
                        "parallelism": "single"},
             "roofline": {"bound": "hbm", "kernel": "k_gather", "achieved": gbs / world, "peak": peak[0],
+                         "unit": "GB/s", "frac": gbs / world / peak[0], "peak_kind": peak[1], "traffic": None},
+            "gpu_launches": K, "clocks": clocks}
+
+
+def _timed_launches(fn, K, warmup, dev, dist):
+    """Average ms of `fn` over K back-to-back calls (CUDA events on the current
+    stream, max over ranks), with the SM clocks sampled meanwhile."""
+    import torch
+
+    for _ in range(max(3, warmup)):
+        fn()
+    sampler = ClockSampler(dev.index or 0)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)
+    stream = torch.cuda.current_stream(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(K):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    return max_over_ranks(a.elapsed_time(b) / K, dist, dev), clocks
+
+
+def run_prepare(args, dev, rank, world, dist):
+    """The scene transform (gsr_scene_prepare; the reference's CPU loop in
+    loadPly_torch / computeCov3D, pybind.cpp:22-56, 105-117) alone on the
+    3 M Gaussians of plain_3m_1080p: per Gaussian it reads log-scales,
+    quaternion and opacity logit (32 B) and writes opacity and the 3D
+    covariance (28 B).  `value` is GB/s of those 60 bytes per Gaussian."""
+    import torch
+
+    from polysplat_gb300 import scenes
+    from polysplat_gb300._lib import check, lib
+
+    raw, _ = scenes.workload("plain_3m_1080p")
+    P = raw.num
+    t = lambda a: torch.from_numpy(a.reshape(P, -1)).to(dev).contiguous()
+    ls, q, lg = t(raw.log_scales), t(raw.quats), t(raw.opacity_logits)
+    op = torch.empty(P, dtype=torch.float32, device=dev)
+    cov = torch.empty((P, 6), dtype=torch.float32, device=dev)
+    L = lib()
+    sh = torch.cuda.current_stream(dev).cuda_stream
+
+    def launch():
+        check(L.gsr_scene_prepare(P, ls.data_ptr(), q.data_ptr(), lg.data_ptr(), op.data_ptr(), cov.data_ptr(), sh),
+              "scene_prepare")
+
+    K = max(3, args.steps)
+    ms, clocks = _timed_launches(launch, K, args.warmup, dev, dist)
+    if rank != 0:
+        return None
+    per = 32 + 28
+    gbs = world * P * per / (ms * 1e-3) / 1e9
+    peak = measured_peaks()
+    return {"metric": "GB/s", "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "prepare_plain_3m", "gaussians": P, "bytes_per_gaussian": per,
+                       "l2": "%.0f MB per step, %.1fx L2: part of it can stay in L2 between launches"
+                             % (P * per / 1e6, P * per / 129e6), "parallelism": "single"},
+            "roofline": {"bound": "hbm", "kernel": "k_scene_prepare", "achieved": gbs / world, "peak": peak[0],
                          "unit": "GB/s", "frac": gbs / world / peak[0], "peak_kind": peak[1], "traffic": None},
             "gpu_launches": K, "clocks": clocks}
 
