@@ -607,6 +607,30 @@ def run_serve(args, dev, rank, world, dist):
             "gpu_launches": launches, "clocks": clocks}
 
 
+def _timed_launches(fn, K, warmup, dev, dist):
+    """Average ms of `fn` over K back-to-back calls (CUDA events on the current
+    stream, max over ranks), with the SM clocks sampled meanwhile."""
+    import torch
+
+    for _ in range(max(3, warmup)):
+        fn()
+    sampler = ClockSampler(dev.index or 0)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)
+    stream = torch.cuda.current_stream(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(K):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    return max_over_ranks(a.elapsed_time(b) / K, dist, dev), clocks
+
+
 def run_gather(args, dev, rank, world, dist):
     """The feature gather (gather_features; the reference's gather.cu:6-22)
     alone, over the sorted values of one plain_3m_1080p frame: per key, the
@@ -630,24 +654,8 @@ def run_gather(args, dev, rank, world, dist):
     dst = [torch.empty((M, k), device=dev, dtype=torch.float32) for k in (2, 4, 4)]
     src = (rast.points_xy, rast.rgb_depth, rast.conic_opacity)
     per_key = 4 + 2 * sum(t.shape[1] * 4 for t in dst)
-    for _ in range(max(3, args.warmup)):
-        ops.gather_features(M, vals, *src, *dst)
     K = max(3, args.steps)
-    sampler = ClockSampler(dev.index or 0)
-    if dist is not None:
-        dist.barrier()
-    torch.cuda.synchronize()
-    sampler.start()
-    time.sleep(0.3)
-    stream = torch.cuda.current_stream(dev)
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    for _ in range(K):
-        ops.gather_features(M, vals, *src, *dst)
-    b.record(stream)
-    torch.cuda.synchronize()
-    clocks = sampler.stop()
-    ms = max_over_ranks(a.elapsed_time(b) / K, dist, dev)
+    ms, clocks = _timed_launches(lambda: ops.gather_features(M, vals, *src, *dst), K, args.warmup, dev, dist)
     if rank != 0:
         return None
     gbs = world * M * per_key / (ms * 1e-3) / 1e9
@@ -662,30 +670,6 @@ def run_gather(args, dev, rank, world, dist):
             "roofline": {"bound": "hbm", "kernel": "k_gather", "achieved": gbs / world, "peak": peak[0],
                          "unit": "GB/s", "frac": gbs / world / peak[0], "peak_kind": peak[1], "traffic": None},
             "gpu_launches": K, "clocks": clocks}
-
-
-def _timed_launches(fn, K, warmup, dev, dist):
-    """Average ms of `fn` over K back-to-back calls (CUDA events on the current
-    stream, max over ranks), with the SM clocks sampled meanwhile."""
-    import torch
-
-    for _ in range(max(3, warmup)):
-        fn()
-    sampler = ClockSampler(dev.index or 0)
-    if dist is not None:
-        dist.barrier()
-    torch.cuda.synchronize()
-    sampler.start()
-    time.sleep(0.3)
-    stream = torch.cuda.current_stream(dev)
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    for _ in range(K):
-        fn()
-    b.record(stream)
-    torch.cuda.synchronize()
-    clocks = sampler.stop()
-    return max_over_ranks(a.elapsed_time(b) / K, dist, dev), clocks
 
 
 def run_prepare(args, dev, rank, world, dist):
