@@ -1,4 +1,5 @@
 // C ABI of the gsr library (declared in include/gsr.h).
+#include <atomic>
 #include <cstring>
 #include <mutex>
 
@@ -8,15 +9,18 @@ namespace gsr {
 
 int device_sm_count()
 {
-    static int cached[64] = {0};
+    // one query per device; host threads may race to fill it with the same value
+    static std::atomic<int> cached[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
-    if (cached[dev] == 0) {
+    int v = cached[dev].load(std::memory_order_relaxed);
+    if (v == 0) {
         int n = 0;
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        cached[dev] = n > 0 ? n : 1;
+        v = n > 0 ? n : 1;
+        cached[dev].store(v, std::memory_order_relaxed);
     }
-    return cached[dev];
+    return v;
 }
 
 // Stage-timing state: `frames` rows of kMarks events; row g_prof_row is the

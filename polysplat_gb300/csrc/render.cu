@@ -20,6 +20,7 @@
 // skip, front-to-back compositing, and a whole-tile exit once every pixel of
 // the tile has T < 1e-4, checked every CADENCE Gaussians.  Output is the
 // truncating uint8 encode of render.cu:375-394.
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 
@@ -385,11 +386,13 @@ template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool
 cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
 {
     auto kern = k_render<BX, BY, CADENCE, SHADER, DT, RANGE_MODE, TMA, BATCH, EXIT>;
-    static int per_sm = 0;
+    static std::atomic<int> per_sm_cache{0};  // host threads may race to fill it with the same value
+    int per_sm = per_sm_cache.load(std::memory_order_relaxed);
     if (per_sm == 0) {
-        int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kRenderWarps * 32, 0) != cudaSuccess || b < 1) b = 1;
-        per_sm = b;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kRenderWarps * 32, 0) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        per_sm_cache.store(per_sm, std::memory_order_relaxed);
     }
     const int warps_needed = p.tiles;
     int grid = device_sm_count() * per_sm;
@@ -458,15 +461,14 @@ static cudaError_t launch_prepared(const RenderArgs& a, RenderParams& p, cudaStr
 
 static bool use_render_tma()
 {
-    static int mode = -1;
-    if (mode < 0) {
-        // per-thread cp.async staging measured faster than per-lane 16-byte
-        // bulk copies (28 vs 48 us at 1080p, 2.5 vs 3.6 ms at 8K): bulk
-        // copies only on request
+    // per-thread cp.async staging measured faster than per-lane 16-byte bulk
+    // copies (28 vs 48 us at 1080p, 2.5 vs 3.6 ms at 8K): bulk copies only on
+    // request (read once, thread-safe initialisation)
+    static const bool tma = [] {
         const char* e = getenv("GSR_RENDER_TMA");
-        mode = (e && strcmp(e, "1") == 0) ? 1 : 0;
-    }
-    return mode == 1;
+        return e && strcmp(e, "1") == 0;
+    }();
+    return tma;
 }
 
 // ---------------------------------------------------------------------------

@@ -27,6 +27,7 @@
 // destination buffer on the device so that the last working pass lands in the
 // output.
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 
@@ -419,11 +420,10 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortJob<K> a, int pass
 // "match" (1) everywhere
 int sort_rank_mode()
 {
-    static int mode = -1;
-    if (mode < 0) {
+    static const int mode = [] {  // read once, thread-safe initialisation
         const char* e = getenv("GSR_SORT_RANK");
-        mode = (e && strcmp(e, "ballot") == 0) ? 0 : (e && strcmp(e, "match") == 0) ? 1 : 2;
-    }
+        return (e && strcmp(e, "ballot") == 0) ? 0 : (e && strcmp(e, "match") == 0) ? 1 : 2;
+    }();
     return mode;
 }
 
@@ -449,19 +449,19 @@ cudaError_t run_sort(const SortJob<K>& a, int max_passes, cudaStream_t stream)
     const int forced = sort_rank_mode();
     const int mode = forced != 2 ? forced : (mixed ? 2 : 1);
     auto kern = mode == 0 ? k_pass<K, 0> : mode == 1 ? k_pass<K, 1> : k_pass<K, 2>;
-    static bool attr_set[3] = {false, false, false};
+    // per ranking mode: the shared-memory attribute, then the occupancy; host
+    // threads may race to fill these with the same values
+    static std::atomic<int> per_sm_cache[3];
     const int smem = (int)sizeof(PassSmem<K>);
-    if (!attr_set[mode]) {
+    int per_sm = per_sm_cache[mode].load(std::memory_order_acquire);
+    if (per_sm == 0) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        attr_set[mode] = true;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSortThreads, smem) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        per_sm_cache[mode].store(per_sm, std::memory_order_release);
     }
-    static int per_sm[3] = {0, 0, 0};
-    if (per_sm[mode] == 0) {
-        int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kSortThreads, smem) != cudaSuccess || b < 1) b = 1;
-        per_sm[mode] = b;
-    }
-    const int grid = (int)std::min<long long>((long long)sms * per_sm[mode], std::max<long long>(1, a.s.tiles_cap));
+    const int grid = (int)std::min<long long>((long long)sms * per_sm, std::max<long long>(1, a.s.tiles_cap));
     for (int p = 0; p < max_passes; p++) {
         kern<<<grid, kSortThreads, smem, stream>>>(a, p);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
