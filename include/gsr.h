@@ -335,7 +335,8 @@ gsr_status gsr_batcher_set_thresholds(gsr_batcher* b, int massive_area, int huge
  * when the variant needs them, render).  gsr_profile_read() synchronises and
  * writes the stage durations in ms, row f = frame f, `max_stages` columns,
  * and returns the number of stages per frame (or -1).  gsr_profile_end()
- * stops recording and frees the events. */
+ * stops recording and frees the events.  The recording state is
+ * process-wide: one session at a time, driven from one host thread. */
 gsr_status gsr_profile_begin(int frames);
 int gsr_profile_read(float* ms, int frames, int max_stages);
 void gsr_profile_end(void);
