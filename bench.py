@@ -53,7 +53,9 @@ E2E_VARIANT = "preranges_smem_persistent_lite_e2e"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps: frames (plain-forward workloads, default 500) or saturated passes over the "
+                         "request stream (serve_mix, default 10)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", default="serve_mix",
                     help="serve_mix (config 3, the headline), or a plain-forward workload: plain_3m_1080p, "
@@ -194,13 +196,14 @@ def run_reference(args):
         # the request stream in order on the host cores (the reference has
         # no CPU path: its algorithm restated in FP64), bounded to about a minute
         raws, reqs = scenes.serve_mix()
-        cpu = serve_cpu_baseline(raws, reqs[: max(1, args.steps)], seconds=60.0)
+        cpu = serve_cpu_baseline(raws, reqs[:CPU_SAMPLE_REQUESTS], seconds=60.0)
         line = {"impl": "reference", "metric": "frames/s", "value": cpu["value"], "unit": "frames/s",
                 "n_gpus": world, "steps": cpu["requests"], "warmup": 0,
-                "ms_per_step": 1000.0 / cpu["value"], "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": "serve_mix", "scenes_gaussians": [r.num for r in raws],
-                           "requests": len(reqs)},
+                "step": "one request of the stream, on the host cores (a bounded sample: its first %d requests)"
+                        % CPU_SAMPLE_REQUESTS,
+                "ms_per_step": 1000.0 / cpu["value"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": serve_config(raws, reqs, world),
                 "cpu_baseline": cpu,
                 "e2e": {"value": cpu["value"], "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
@@ -506,61 +509,170 @@ def run_serve_profile(args, dev):
     return {"workload": "serve_mix (profiling run)", "tuned": dataclasses.asdict(cfg), "served": st.as_dict()}
 
 
+def _img_cmp(a, b):
+    """max-abs (in 1/255), differing pixels and PSNR of two uint8 images on the device."""
+    import math
+
+    d = (a.int() - b.int()).abs()
+    mse = float((d.double() ** 2).mean())
+    return int(d.max()), int((d > 0).sum()), (10.0 * math.log10(255.0 ** 2 / mse)) if mse > 0 else float("inf")
+
+
+def stream_parity(scs, reqs, served, plain, dev):
+    """Every request's served image and plain-forward image against the
+    reference build's own E2E render of the same request (its preprocess
+    and fused render kernels built from its sources, and its CUB sort call,
+    on this GPU).  Bar per request: max-abs <= 2/255 and PSNR >= 50 dB."""
+    import torch
+
+    from oracle import refkernels as RK
+
+    if not RK.available():
+        return {"unavailable": "reference device images not built"}
+    cap = max(1 << 20, int(1.25 * max(n for _, n in plain)))
+    pipe = RK.Pipeline(max(scs, key=lambda s: s.num_vertex), reqs[0].camera, cap)
+    rows = {"served": [], "plain": []}
+    for r, img_s, (img_p, n) in zip(reqs, served, plain):
+        pipe.set_view(scs[r.scene], r.camera)
+        m = pipe.forward()
+        if m != n:
+            rows.setdefault("key_count_mismatch", []).append((r.camera.id, m, n))
+        for name, img in (("served", img_s), ("plain", img_p)):
+            rows[name].append((r.camera.id, r.camera.width) + _img_cmp(img, pipe.out))
+    del pipe
+    torch.cuda.empty_cache()
+
+    def summary(rs):
+        fails = [x for x in rs if x[2] > 2 or x[4] < 50.0]
+        worst = min(rs, key=lambda x: x[4])
+        return {"requests": len(rs), "identical": sum(1 for x in rs if x[2] == 0),
+                "fail_bar": len(fails), "worst_max_abs": max(x[2] for x in rs),
+                "min_psnr_db": None if worst[4] == float("inf") else round(worst[4], 2),
+                "worst_request": {"id": worst[0], "width": worst[1], "max_abs": worst[2], "pixels_differ": worst[3]},
+                "failures": [{"id": x[0], "width": x[1], "max_abs": x[2], "pixels_differ": x[3],
+                              "psnr_db": round(x[4], 2)} for x in fails[:8]]}
+
+    out = {"served_vs_reference": summary(rows["served"]), "plain_vs_reference": summary(rows["plain"]),
+           "bar": "max-abs <= 2/255 and PSNR >= 50 dB per request",
+           "reference": "the reference's E2E forward (preprocessCUDA, CUB SortPairs, "
+                        "renderCUDA_preranges_smem_persistent_lite_fused, 16x16 tiles), built from its sources"}
+    if "key_count_mismatch" in rows:
+        out["key_count_mismatch"] = rows["key_count_mismatch"][:8]
+    return out
+
+
+def serve_config(raws, reqs, world):
+    """The serve_mix workload's config (shared by both arms of the bench)."""
+    return {"workload": "serve_mix", "step": "one saturated pass over the 512-request stream",
+            "scenes_gaussians": [r.num for r in raws], "requests": len(reqs), "arrival": "Poisson 240/s",
+            "resolutions": ["1280x720", "1920x1080", "2560x1440", "3840x2160"], "budget_gb": 60, "sh": "fp16",
+            "tile": "16x16", "render": "preranges_smem_persistent_lite_e2e (exit check every 16 Gaussians)",
+            "l2": "scenes of 0.5-10 M Gaussians (68 MB-1.4 GB), larger than L2",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
+# CPU sample of the serve_mix stream: its first requests, in order
+CPU_SAMPLE_REQUESTS = 20
+
+
 def run_serve(args, dev, rank, world, dist):
     """Config 3: resident scenes of 0.5/2/5/10 M Gaussians, 512 requests
     arriving by a Poisson process at 240/s, resolutions 720p-2160p, 60 GB
-    admission budget.  The plain per-request forward against the served,
-    continuously batched path (tuned by the autotuner on a 128-request
-    sample), both saturated (all requests queued at once: capacity) and in
-    real time (latency).  `value` is the served capacity with every image
-    delivered to pinned host memory."""
+    admission budget.  A step is one saturated pass over the whole stream
+    (all 512 requests queued at once), served through Server.run with every
+    image delivered to pinned host memory; `value` is frames/s over the K
+    timed passes.  The plain per-request forward (the reference's usage of
+    Rasterizer.forward) is timed the same way, and both run once more in
+    real time for latency.  Every served and plain image of the stream is
+    compared with the reference build's own render of the same request."""
     import gc
 
     import torch
 
-    from polysplat_gb300 import Scene, scenes
+    from polysplat_gb300 import Camera, Rasterizer, Scene, scenes
     from polysplat_gb300.serving import PlainServer, Server, autotune
 
     budget = 60 << 30
     raws, reqs = scenes.serve_mix()
     scs = [Scene.from_raw(r, dev) for r in raws]
     torch.cuda.synchronize()
-    sampler = ClockSampler(dev.index or 0)
+    K = max(1, args.steps if args.steps is not None else 10)
+    W = max(3, args.warmup)
+    log = (lambda m: print(m, file=sys.stderr, flush=True)) if rank == 0 else None
 
-    # plain per-request forward (the reference's usage of Rasterizer.forward)
+    def timed_pass(fn):
+        """One pass bracketed by device synchronisation and CUDA events on
+        the current stream (the passes run on several streams)."""
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        st = fn()
+        torch.cuda.synchronize()
+        b.record()
+        b.synchronize()
+        return st, a.elapsed_time(b) / 1000.0
+
+    # plain per-request forward
     plain = PlainServer(scs, 1 << 28, dev)
     plain.run(reqs[:16], realtime=False)
-    p_sat, _ = plain.run(reqs, realtime=False)
+    p_walls = [timed_pass(lambda: plain.run(reqs, realtime=False)[0])[1] for _ in range(3)]
     p_rt, _ = plain.run(reqs, realtime=True)
     del plain
     gc.collect()
     torch.cuda.empty_cache()
 
-    log = (lambda m: print(m, file=sys.stderr, flush=True)) if rank == 0 else None
     best, table = autotune(scs, reqs[:128], dev, budget_bytes=budget, log=log)
     srv = Server(scs, dev, budget, best)
-    # warm-up over the whole request stream: every batch shape's graph is
-    # captured and the pinned host pool holds a buffer for every request in
-    # flight, so the timed runs measure steady-state serving (a pinned
-    # allocation costs milliseconds and would otherwise land in the timed run)
-    warm_passes = max(1, args.warmup // 3)
-    for _ in range(warm_passes):
+    # warm-up passes over the whole stream: every batch shape's graph is
+    # captured and the pinned host pool holds a buffer for every request
+    for _ in range(W):
         srv.run(reqs, realtime=False, deliver=True)
         for r in reqs:
             srv.release(r)
+    sampler = ClockSampler(dev.index or 0)
     if dist is not None:
         dist.barrier()
     sampler.start()
-    s_sat = srv.run(reqs, realtime=False, deliver=True)
-    for r in reqs:
-        srv.release(r)
+    time.sleep(0.3)
+    walls, last = [], None
+
+    def one():
+        st = srv.run(reqs, realtime=False, deliver=True)
+        for r in reqs:
+            srv.release(r)
+        return st
+
+    for _ in range(K):
+        last, w = timed_pass(one)
+        walls.append(w)
+    clocks = sampler.stop()
     s_rt = srv.run(reqs, realtime=True, deliver=True)
     for r in reqs:
         srv.release(r)
-    clocks = sampler.stop()
     s_dev = srv.run(reqs, realtime=False, deliver=False)
+    served_imgs = [r.out for r in reqs]
     srv.close()
     del srv
+    gc.collect()
+    torch.cuda.empty_cache()
+
+    # parity of the whole stream against the reference build (untimed)
+    parity = None
+    if not args.quick and world == 1:
+        rast = Rasterizer(max(scs, key=lambda s: s.num_vertex), 1 << 28, 1 << 17)
+        plain_imgs = []
+        for r in reqs:
+            img, st = rast.forward(scs[r.scene], Camera.from_spec(r.camera), torch.zeros(3),
+                                   render_variant=E2E_VARIANT, return_stats=True)
+            plain_imgs.append((img.clone(), int(st["num_rendered"])))
+        del rast
+        torch.cuda.empty_cache()
+        try:
+            parity = stream_parity(scs, reqs, served_imgs, plain_imgs, dev)
+        except Exception as exc:  # informative; the images are checked by the tests too
+            parity = {"unavailable": str(exc)[:200]}
+        del plain_imgs
+    del served_imgs
     gc.collect()
     torch.cuda.empty_cache()
 
@@ -572,39 +684,50 @@ def run_serve(args, dev, rank, world, dist):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = serve_cpu_baseline(raws, reqs, seconds=15.0)
-    wall = s_sat.wall_s
-    wall = max_over_ranks(wall, dist, dev)
-    value = world * len(reqs) / wall
-    img_bytes = sum(r.camera.width * r.camera.height * 3 for r in reqs) / len(reqs)
-    # kernel launches of the saturated run: small batches (preprocess, large-
-    # Gaussian emission, upsweep, 6 digit passes, ranges, render) and large
-    # frames (20 launches of the depth-first forward)
-    launches = s_sat.batches * 11 + s_sat.large * 20
+        cpu = serve_cpu_baseline(raws, reqs[:CPU_SAMPLE_REQUESTS], seconds=60.0)
+    total = max_over_ranks(sum(walls), dist, dev)
+    value = world * K * len(reqs) / total
+    per_pass = sorted(len(reqs) / w for w in walls)
+    p_fps = sorted(len(reqs) / w for w in p_walls)
+    img_bytes = sum(r.camera.width * r.camera.height * 3 for r in reqs)
+    # kernel launches of one saturated pass: small batches (preprocess,
+    # large-Gaussian emission, upsweep, 6 digit passes, ranges, render) and
+    # large frames (20 launches of the depth-first forward)
+    launches = K * (last.batches * 11 + last.large * 20)
     if rank != 0:
         return None
-    return {"metric": "frames/s", "value": value, "unit": "frames/s", "n_gpus": world, "steps": len(reqs),
-            "warmup": warm_passes * len(reqs), "ms_per_step": 1000.0 * wall / len(reqs), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "serve_mix", "scenes_gaussians": [r.num for r in raws], "requests": len(reqs),
-                       "arrival": "Poisson 240/s", "resolutions": ["1280x720", "1920x1080", "2560x1440",
-                                                                   "3840x2160"],
-                       "budget_gb": 60, "tuned": dataclasses.asdict(best), "sh": "fp16",
-                       "l2": "scenes of 0.5-10 M Gaussians (68 MB-1.4 GB), larger than L2",
-                       "parallelism": "replicas" if world > 1 else "single"},
-            "served": {"saturated": s_sat.as_dict(), "realtime_240hz": s_rt.as_dict(),
-                       "saturated_device_only": s_dev.as_dict()},
-            "plain": {"saturated": p_sat.as_dict(), "realtime_240hz": p_rt.as_dict()},
-            "speedup_vs_plain": {"saturated_frames_per_s": s_sat.frames_per_s / p_sat.frames_per_s,
-                                 "realtime_p99": p_rt.p99_ms / s_rt.p99_ms},
-            "autotune": [{"config": c, "frames_per_s": f} for c, f in table],
-            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 376,
-                    "d2h_bytes_per_step": int(img_bytes)},
+    med = statistics.median
+    return {"metric": "frames/s", "value": value, "unit": "frames/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": 1000.0 * total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": serve_config(raws, reqs, world),
+            "gpu_launches": launches, "clocks": clocks, "cpu_baseline": cpu,
             "roofline": dict(fwd["roofline"], workload="plain_3m_1080p (config 1 forward)") if fwd else None,
             "forward": {k: fwd[k] for k in ("value", "ms_per_step", "stages_ms", "e2e", "reference_gpu", "config")}
             if fwd else None,
-            "cpu_baseline": cpu,
-            "gpu_launches": launches, "clocks": clocks}
+            "autotune": {"candidates": len(table), "sample_requests": 128,
+                         "best_sample_frames_per_s": max(f for _, f in table)},
+            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 376 * len(reqs),
+                    "d2h_bytes_per_step": int(img_bytes)},
+            "served": {"tuned": dataclasses.asdict(best),
+                       "saturated_frames_per_s": {"median": med(per_pass), "min": per_pass[0], "max": per_pass[-1],
+                                                  "passes": K},
+                       "device_only_frames_per_s": s_dev.frames_per_s, "batches_per_pass": last.batches,
+                       "large_lane_per_pass": last.large, "retries": last.retries, "failed": last.failed,
+                       "realtime_240hz": {"p50_ms": s_rt.p50_ms, "p99_ms": s_rt.p99_ms,
+                                          "p99_1080p_ms": s_rt.p99_1080p_ms, "frames_per_s": s_rt.frames_per_s}},
+            "plain": {"saturated_frames_per_s": {"median": med(p_fps), "min": p_fps[0], "max": p_fps[-1],
+                                                 "passes": len(p_fps)},
+                      "realtime_240hz": {"p50_ms": p_rt.p50_ms, "p99_ms": p_rt.p99_ms,
+                                         "p99_1080p_ms": p_rt.p99_1080p_ms}},
+            "parity_vs_reference": parity,
+            "headline": {"served_frames_per_s": value, "plain_frames_per_s": med(p_fps),
+                         "speedup_vs_plain": value / med(p_fps), "served_p99_1080p_ms": s_rt.p99_1080p_ms,
+                         "served_p99_ms": s_rt.p99_ms, "plain_p99_ms": p_rt.p99_ms,
+                         "served_min_psnr_vs_reference_db": (parity or {}).get("served_vs_reference", {}).get(
+                             "min_psnr_db"),
+                         "served_requests_failing_bar": (parity or {}).get("served_vs_reference", {}).get(
+                             "fail_bar")}}
 
 
 def _timed_launches(fn, K, warmup, dev, dist):
@@ -844,6 +967,8 @@ def run_reference_gpu(args):
 
 def main():
     args = parse()
+    if args.steps is None and args.workload != "serve_mix":
+        args.steps = 500
     if args.impl == "reference":
         return run_reference(args)
     if args.impl == "reference-gpu":

@@ -52,6 +52,19 @@ typedef enum {
                                          top and bottom 8-row halves stop independently; 16-row tiles only */
 } gsr_render_variant;
 
+/* Flag OR-ed into the variant of gsr_forward and gsr_batcher_render (16x16
+ * tiles; not with GSR_RENDER_SPLIT).  No counterpart in the reference: the
+ * sort handles one key per 2x2 group of 16x16 tiles ("quad") instead of one
+ * per tile.  A key's tile id names the quad (quads numbered row-major,
+ * ceil(ceil(W/16)/2) per row); bits 28-31 of its value mark which of the
+ * quad's tiles, (x & 1) | (y & 1) << 1, the Gaussian hits by the per-tile
+ * emission's own test, and bits 0-27 hold the Gaussian's index (so P must be
+ * below 2^28).  The render blends each 16x16 tile from the Gaussians with
+ * its bit, in key order, which is that tile's per-tile list: the image is
+ * the per-tile pipeline's, with fewer keys to sort.  The key and value
+ * buffers then hold quad keys, not the reference's per-tile keys. */
+#define GSR_QUAD_KEYS 0x100
+
 /* Library version and a check that a CUDA device of compute capability 10.3
  * is present (returns GSR_CUDA_ERROR otherwise). */
 int gsr_version(void);
@@ -133,6 +146,12 @@ gsr_status gsr_sort_bits(int num, const int32_t* d_num, int end_bit, void* works
 gsr_status gsr_sort_bits_static(int num, const int32_t* d_num, int end_bit, const uint64_t* keys_in,
                                 const uint32_t* values_in, uint64_t* keys_out, uint32_t* values_out,
                                 int64_t capacity, gsr_stream_t stream);
+/* Device-side outcome of the last gsr_sort_bits_static on `stream`: waits for
+ * the stream and reads the static array's status word (no allocation).
+ * GSR_TIMEOUT when a bounded look-back wait ran out (the output is then not
+ * sorted), else GSR_OK.  The word is shared like the array: read it before
+ * the next static sort starts.  No counterpart in the reference. */
+gsr_status gsr_sort_bits_static_status(gsr_stream_t stream);
 
 /* ---- tile ranges / gather ----------------------------------------------- */
 /* ranges[t] = [first, end) of tile t in the sorted keys.  scan_semantics = 0
@@ -343,6 +362,20 @@ void gsr_profile_end(void);
 
 /* Text of the last CUDA error seen by the library (for diagnostics). */
 const char* gsr_last_error(void);
+
+/* ---- failure-detection hooks ---------------------------------------------- */
+/* No counterpart in the reference.  Process-wide switches that let a test
+ * make a bounded device wait run out, so that the timeout path can be checked
+ * on a GPU without faulting or hanging it.  gsr_debug_set_sort_wait_limit
+ * sets how many times the radix sort's look-back re-reads an unpublished
+ * entry before it gives up (0 restores the default, about a second of
+ * waiting).  gsr_debug_stall_sort(1) makes the first digit pass of every
+ * later sort leave its tile 0 untaken, so the tiles after it wait on an entry
+ * that is never published; the sort then reports GSR_TIMEOUT through the
+ * status word (gsr_read_status / gsr_sort_bits_static_status) and writes
+ * nothing outside its buffers.  Both apply to sorts launched after the call. */
+gsr_status gsr_debug_set_sort_wait_limit(uint32_t spins);
+gsr_status gsr_debug_stall_sort(int on);
 
 #ifdef __cplusplus
 }

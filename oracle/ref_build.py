@@ -1,6 +1,7 @@
 """Recipe for the reference-kernel runner -- TEST INFRASTRUCTURE.
 
-Where the reference sources are present (``/root/reference``, read-only), its
+Where the reference sources are present (``GSR_REFERENCE_DIR``, default
+``/root/reference``; read-only), its
 ``csrc/cuda_rasterizer/preprocess.cu`` and ``render.cu`` are compiled exactly
 as they lie, with the reference's own nvcc flags (setup.py:20) plus the
 sm_103a target, into device images under ``oracle/_ref/`` (git-ignored; the
@@ -17,7 +18,7 @@ import shutil
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+REF = os.environ.get("GSR_REFERENCE_DIR", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
 RUNNER = os.path.join(HERE, "_build", "librefrun.so")
 REF_NVCC_FLAGS = ["-O3", "--use_fast_math", "--extra-device-vectorization", "-Xptxas=-O3", "-std=c++17"]

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -260,6 +261,147 @@ int ref_sort(int n, int end_bit, void* temp, size_t temp_bytes, const void* keys
                                                     (const uint32_t*)vals_in, (uint32_t*)vals_out, n, 0, end_bit,
                                                     (cudaStream_t)stream);
     return e == cudaSuccess ? 0 : 70 + (int)e;
+}
+
+// ---- the reference's ES ("early sorting") steps (csrc/pybind.cpp:183-330) ----
+// Pass A and pass B are the reference's kernels from the cubin, launched as
+// its host wrappers do (preprocess.cu:1335-1446: grid (P + 127) / 128, block
+// (8, 4, 4)).  The steps between them are the CUB calls of sort.cu:204-285
+// issued through CUB's public entry points, with this file's own one-line
+// helper kernels for the identity, gather, total and key-rebuild steps.
+
+// preprocess_es_pass_a{,_half_sh} (preprocess.cu:1335-1402)
+int ref_es_pass_a(int P, const void* pos, const void* opacity, const void* shs, int shs_half, const float* view16,
+                  const float* proj16, const float* campos3, int W, int H, int bx, int by, float tanx, float tany,
+                  float fx, float fy, void* xy, void* cov3d, void* rgbd, void* con, void* tiles_per_gauss,
+                  void* conic_power_raw, void* depth_natural, void* rect_bounds, void* stream)
+{
+    CUfunction f = find(g_pre, "23preprocessCUDA_ES_PassAE");
+    if (!f) return 11;
+    if (P <= 0) return 0;
+    unsigned char half = shs_half ? 1 : 0;
+    float view[16], proj[16], cam[3];
+    memcpy(view, view16, sizeof view);
+    memcpy(proj, proj16, sizeof proj);
+    memcpy(cam, campos3, sizeof cam);
+    unsigned grid[3] = {(unsigned)((W + bx - 1) / bx), (unsigned)((H + by - 1) / by), 1u};
+    void* packed = nullptr;
+    void* args[] = {&P,    (void*)&pos, (void*)&opacity, (void*)&shs, &half,          view,
+                    proj,  cam,         &W,              &H,          &bx,            &by,
+                    &tanx, &tany,       &fx,             &fy,         &xy,            &cov3d,
+                    &rgbd, &con,        &packed,         &tiles_per_gauss, &conic_power_raw, &depth_natural,
+                    &rect_bounds, grid};
+    CUresult r = cuLaunchKernel(f, (P + 127) / 128, 1, 1, 8, 4, 4, 0, (CUstream)stream, args, nullptr);
+    return r == CUDA_SUCCESS ? 0 : 20 + (int)r;
+}
+
+// preprocess_es_pass_b (preprocess.cu:1407-1446)
+int ref_es_pass_b(int P, int W, int H, int bx, int by, const void* perm, const void* cum, const void* tpg_sorted,
+                  const void* xy, const void* cpr, const void* rb, void* tile_keys, void* vals, void* stream)
+{
+    CUfunction f = find(g_pre, "23preprocessCUDA_ES_PassBE");
+    if (!f) return 12;
+    if (P <= 0) return 0;
+    unsigned grid[3] = {(unsigned)((W + bx - 1) / bx), (unsigned)((H + by - 1) / by), 1u};
+    void* args[] = {&P,          &bx,         &by,        (void*)&perm, (void*)&cum,    (void*)&tpg_sorted,
+                    (void*)&xy,  (void*)&cpr, (void*)&rb, &tile_keys,   &vals,          grid};
+    CUresult r = cuLaunchKernel(f, (P + 127) / 128, 1, 1, 8, 4, 4, 0, (CUstream)stream, args, nullptr);
+    return r == CUDA_SUCCESS ? 0 : 20 + (int)r;
+}
+
+}  // extern "C"
+
+namespace {
+__global__ void es_identity(int P, uint32_t* id)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P) id[i] = (uint32_t)i;
+}
+__global__ void es_gather(int P, const uint32_t* perm, const int32_t* src, int32_t* dst)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P) dst[i] = src[perm[i]];
+}
+__global__ void es_total(int P, const int32_t* cum, const int32_t* cnt, int32_t* out)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) *out = P > 0 ? cum[P - 1] + cnt[P - 1] : 0;
+}
+__global__ void es_rebuild(int M, const uint32_t* t32, uint64_t* k64)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < M) k64[i] = (uint64_t)t32[i] << 32;
+}
+unsigned higher_msb(unsigned n)  // getHigherMsb (sort.cu:14-29)
+{
+    unsigned msb = 16, step = 16;
+    while (step > 1) {
+        step /= 2;
+        if (n >> msb) msb += step;
+        else msb -= step;
+    }
+    if (n >> msb) msb++;
+    return msb;
+}
+}  // namespace
+
+extern "C" {
+
+// Temporary bytes of the three CUB calls (sort.cu:127-149, 186-191).
+size_t ref_es_depth_sort_temp_bytes(int P)
+{
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairs<float, uint32_t>(nullptr, b, nullptr, nullptr, nullptr, nullptr, P, 0, 32);
+    return b;
+}
+size_t ref_es_scan_temp_bytes(int P)
+{
+    size_t b = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, b, (int32_t*)nullptr, (int32_t*)nullptr, P);
+    return b;
+}
+size_t ref_es_tile_sort_temp_bytes(int M)
+{
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairs<uint32_t, uint32_t>(nullptr, b, nullptr, nullptr, nullptr, nullptr, M, 0, 32);
+    return b;
+}
+
+// es_depth_sort_and_scan (sort.cu:204-245)
+int ref_es_depth_sort_and_scan(int P, const void* tiles_per_gauss, const void* depth_natural, void* identity,
+                               void* perm, void* depth_sorted, void* tpg_sorted, void* cum, void* total,
+                               void* sort_temp, size_t sort_bytes, void* scan_temp, size_t scan_bytes, void* stream)
+{
+    if (P <= 0) return 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nb = (P + 255) / 256;
+    es_identity<<<nb, 256, 0, s>>>(P, (uint32_t*)identity);
+    size_t b = sort_bytes;
+    cudaError_t e = cub::DeviceRadixSort::SortPairs<float, uint32_t>(
+        sort_temp, b, (const float*)depth_natural, (float*)depth_sorted, (const uint32_t*)identity, (uint32_t*)perm, P,
+        0, 32, s);
+    if (e != cudaSuccess) return 80 + (int)e;
+    es_gather<<<nb, 256, 0, s>>>(P, (const uint32_t*)perm, (const int32_t*)tiles_per_gauss, (int32_t*)tpg_sorted);
+    b = scan_bytes;
+    e = cub::DeviceScan::ExclusiveSum(scan_temp, b, (const int32_t*)tpg_sorted, (int32_t*)cum, P, s);
+    if (e != cudaSuccess) return 90 + (int)e;
+    es_total<<<1, 32, 0, s>>>(P, (const int32_t*)cum, (const int32_t*)tpg_sorted, (int32_t*)total);
+    return cudaGetLastError() == cudaSuccess ? 0 : 99;
+}
+
+// es_tile_sort (sort.cu:248-285)
+int ref_es_tile_sort(int M, int W, int H, int bx, int by, const void* tk_u, const void* v_u, void* tk_s, void* v_s,
+                     void* keys64, void* temp, size_t temp_bytes, void* stream)
+{
+    if (M <= 0) return 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    const unsigned tiles = (unsigned)(((W + bx - 1) / bx) * ((H + by - 1) / by));
+    size_t b = temp_bytes;
+    cudaError_t e = cub::DeviceRadixSort::SortPairs<uint32_t, uint32_t>(
+        temp, b, (const uint32_t*)tk_u, (uint32_t*)tk_s, (const uint32_t*)v_u, (uint32_t*)v_s, M, 0,
+        (int)higher_msb(tiles), s);
+    if (e != cudaSuccess) return 80 + (int)e;
+    es_rebuild<<<(M + 255) / 256, 256, 0, s>>>(M, (const uint32_t*)tk_s, (uint64_t*)keys64);
+    return cudaGetLastError() == cudaSuccess ? 0 : 99;
 }
 
 // The reference's E2E forward (csrc/pybind.cpp:1085-1149): memset counter,

@@ -24,6 +24,7 @@ RENDER_DEFAULT = 2
 RENDER_RANGES_CADENCE2 = 3
 RENDER_DT = 4
 RENDER_SPLIT = 5
+QUAD_KEYS = 0x100  # GSR_QUAD_KEYS: one key per 2x2 group of 16x16 tiles
 
 
 class GsrError(RuntimeError):
@@ -59,6 +60,9 @@ def _declare(L):
                          P, P, sz, P, P, P, P, i64, P, P, P, P, P, P, P], i32),
     }
     sig["gsr_sort_bits_static"] = ([i32, P, i32, P, P, P, P, i64, P], i32)
+    sig["gsr_sort_bits_static_status"] = ([P], i32)
+    sig["gsr_debug_set_sort_wait_limit"] = ([ctypes.c_uint32], i32)
+    sig["gsr_debug_stall_sort"] = ([i32], i32)
     sig["gsr_batcher_device_bytes"] = ([i32, i64, i64, i32], sz)
     sig["gsr_batcher_create"] = ([i32, i64, i64, i32], P)
     sig["gsr_batcher_destroy"] = ([P], None)

@@ -29,11 +29,11 @@ namespace {
 constexpr int kStagingSlots = 4;
 
 struct Shape {
-    int variant, half, bx, by, n_views, blocks, tiles;
+    int variant, half, bx, by, n_views, blocks, tiles, quad;  // tiles: key tile ids (quads when quad)
     bool operator<(const Shape& o) const
     {
-        return std::tie(variant, half, bx, by, n_views, blocks, tiles) <
-               std::tie(o.variant, o.half, o.bx, o.by, o.n_views, o.blocks, o.tiles);
+        return std::tie(variant, half, bx, by, n_views, blocks, tiles, quad) <
+               std::tie(o.variant, o.half, o.bx, o.by, o.n_views, o.blocks, o.tiles, o.quad);
     }
 };
 
@@ -103,8 +103,8 @@ bool valid_shape(int bx, int by) { return (bx == 16 && by == 16) || (bx == 32 &&
 
 // Fill the parameter block of one view (the same fields the single-view
 // preprocess entry fills), plus its offsets into the batch.
-void pack_view(PreprocessParams& p, const gsr_scene_ref& sc, const gsr_view& v, int bx, int by, gsr_batcher* b,
-               int gid_base, int tile_base)
+void pack_view(PreprocessParams& p, const gsr_scene_ref& sc, const gsr_view& v, int bx, int by, bool quad,
+               gsr_batcher* b, int gid_base, int tile_base)
 {
     std::memset(&p, 0, sizeof(p));
     WorkspaceHeader* h = reinterpret_cast<WorkspaceHeader*>(b->ws);
@@ -148,6 +148,7 @@ void pack_view(PreprocessParams& p, const gsr_scene_ref& sc, const gsr_view& v, 
     p.n_views = 0;  // set per batch in the base block
     p.massive_area = b->massive_area;
     p.huge_area = b->huge_area;
+    p.quad = quad ? 1 : 0;
 }
 
 // The kernel sequence of a batch (everything after the parameter copy).
@@ -173,6 +174,7 @@ cudaError_t enqueue(gsr_batcher* b, const Shape& s, cudaStream_t st)
     base.n_views = s.n_views;
     base.bx = s.bx;
     base.by = s.by;
+    base.quad = s.quad;
     e = launch_preprocess_views(base, s.n_views, s.blocks, s.half != 0, st);
     if (e != cudaSuccess) return e;
     SortArgs sa;
@@ -207,6 +209,7 @@ cudaError_t enqueue(gsr_batcher* b, const Shape& s, cudaStream_t st)
     ra.vals = b->vs;
     ra.ranges = b->ranges;
     ra.ws = h;
+    ra.quad = s.quad;
     return launch_render_views(ra, b->d_views, s.n_views, s.tiles, st);
 }
 
@@ -288,7 +291,16 @@ gsr_status gsr_batcher_render(gsr_batcher* b, int variant, int shs_half, int blo
                               int use_graph, gsr_stream_t stream)
 {
     if (!b || !scenes || !views || n_views <= 0 || n_views > b->max_views || n_scenes <= 0) return GSR_INVALID_ARG;
+    const bool quad = (variant & GSR_QUAD_KEYS) != 0;  // one key per 2x2 group of 16x16 tiles
+    variant &= ~GSR_QUAD_KEYS;
     if (!valid_shape(block_x, block_y) || variant < 0 || variant > GSR_RENDER_DT) return GSR_INVALID_ARG;
+    if (quad && (block_x != 16 || block_y != 16 || b->max_gaussians > (long long)kQuadGidMask + 1))
+        return GSR_INVALID_ARG;
+    // key tile ids of one view: its tiles, or its quads
+    auto key_tiles = [&](int w, int h, int& gx) {
+        gx = quad ? quad_cols(div_up(w, 16)) : div_up(w, block_x);
+        return gx * (quad ? quad_cols(div_up(h, 16)) : div_up(h, block_y));
+    };
     cudaStream_t st = (cudaStream_t)stream;
     std::lock_guard<std::mutex> lk(b->mu);
     // layout of the batch: first feature slot and first tile of every view
@@ -301,7 +313,8 @@ gsr_status gsr_batcher_render(gsr_batcher* b, int variant, int shs_half, int blo
         if (sc.P < 0 || (sc.P > 0 && (!sc.pos || !sc.shs || !sc.opacity || !sc.cov3d))) return GSR_INVALID_ARG;
         if (div_up(v.width, block_x) >= 65536) return GSR_INVALID_ARG;
         g += sc.P;
-        tiles += div_up(v.width, block_x) * div_up(v.height, block_y);
+        int gxv = 0;
+        tiles += key_tiles(v.width, v.height, gxv);
         blocks += div_up(sc.P, 256);
         if (g > b->max_gaussians || tiles > b->max_tiles) return GSR_INVALID_ARG;
     }
@@ -317,10 +330,10 @@ gsr_status gsr_batcher_render(gsr_batcher* b, int variant, int shs_half, int blo
     for (int i = 0; i < n_views; i++) {
         const gsr_view& v = views[i];
         const gsr_scene_ref& sc = scenes[v.scene];
-        pack_view(hp[i], sc, v, block_x, block_y, b, (int)gb, tb);
+        pack_view(hp[i], sc, v, block_x, block_y, quad, b, (int)gb, tb);
         RenderView& rv = hv[i];
         rv.tile_base = tb;
-        rv.gx = div_up(v.width, block_x);
+        const int vt = key_tiles(v.width, v.height, rv.gx);
         rv.W = v.width;
         rv.H = v.height;
         rv.bg[0] = v.bg[0];
@@ -329,7 +342,7 @@ gsr_status gsr_batcher_render(gsr_batcher* b, int variant, int shs_half, int blo
         rv.pad = 0;
         rv.out = v.out;
         gb += sc.P;
-        tb += rv.gx * div_up(v.height, block_y);
+        tb += vt;
     }
     cudaError_t e = cudaMemcpyAsync(b->d_pre, hp, (size_t)n_views * sizeof(PreprocessParams), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
@@ -339,7 +352,7 @@ gsr_status gsr_batcher_render(gsr_batcher* b, int variant, int shs_half, int blo
     b->last_total = tiles;
 
     const Shape s{variant, shs_half ? 1 : 0, block_x, block_y, n_views,
-                  div_up(blocks > 0 ? blocks : 1, kBlockBucket) * kBlockBucket, tiles};
+                  div_up(blocks > 0 ? blocks : 1, kBlockBucket) * kBlockBucket, tiles, quad ? 1 : 0};
     if (!use_graph || st == nullptr) {
         e = enqueue(b, s, st);
         return e == cudaSuccess ? GSR_OK : GSR_CUDA_ERROR;

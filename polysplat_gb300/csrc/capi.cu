@@ -7,12 +7,26 @@
 
 namespace gsr {
 
+int current_device()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return -1;
+    return dev;
+}
+
+// Failure-detection hooks: process-wide, read by every later sort launch.
+static std::atomic<uint32_t> g_sort_wait_limit{kSpinLimit};
+static std::atomic<int> g_sort_stall{0};
+
+uint32_t sort_wait_limit() { return g_sort_wait_limit.load(std::memory_order_relaxed); }
+bool sort_stall_first_tile() { return g_sort_stall.load(std::memory_order_relaxed) != 0; }
+
 int device_sm_count()
 {
     // one query per device; host threads may race to fill it with the same value
-    static std::atomic<int> cached[64];
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    static std::atomic<int> cached[kMaxDevices];
+    int dev = current_device();
+    if (dev < 0) dev = 0;
     int v = cached[dev].load(std::memory_order_relaxed);
     if (v == 0) {
         int n = 0;
@@ -125,6 +139,18 @@ int gsr_profile_read(float* ms, int frames, int max_stages)
 }
 
 const char* gsr_last_error(void) { return cudaGetErrorString(g_last_error); }
+
+gsr_status gsr_debug_set_sort_wait_limit(uint32_t spins)
+{
+    g_sort_wait_limit.store(spins ? spins : kSpinLimit, std::memory_order_relaxed);
+    return GSR_OK;
+}
+
+gsr_status gsr_debug_stall_sort(int on)
+{
+    g_sort_stall.store(on ? 1 : 0, std::memory_order_relaxed);
+    return GSR_OK;
+}
 
 gsr_status gsr_device_check(int device)
 {
@@ -241,13 +267,14 @@ static gsr_status preprocess_impl(int P, const float* pos, const void* shs, int 
                                   const float* cam_pos, const float* cam_rot, float fx, float fy, float zfar,
                                   float znear, float* points_xy, float* rgb_depth, float* conic_opacity,
                                   uint64_t* keys, uint32_t* values, int64_t cap, int32_t* curr_offset,
-                                  void* workspace, size_t workspace_bytes, cudaStream_t s)
+                                  void* workspace, size_t workspace_bytes, cudaStream_t s, bool quad = false)
 {
     PreprocessParams p;
     const gsr_status st = preprocess_params(p, P, pos, shs, opacity, cov3d, width, height, block_x, block_y, cam_pos,
                                             cam_rot, fx, fy, zfar, znear, points_xy, rgb_depth, conic_opacity, keys,
                                             values, cap, curr_offset, workspace, workspace_bytes);
     if (st != GSR_OK) return st;
+    p.quad = quad ? 1 : 0;
     return from_cuda(launch_preprocess(p, shs_half != 0, s));
 }
 
@@ -331,10 +358,11 @@ static gsr_status render_impl(int variant, int num, const int32_t* d_num, long l
                               int block_x, int block_y, int P, const float* points_xy, const float* rgb_depth,
                               const float* conic_opacity, const uint64_t* keys_sorted, const uint32_t* values_sorted,
                               const int32_t* ranges, const float* bg_color, uint8_t* out_color, void* workspace,
-                              cudaStream_t s)
+                              cudaStream_t s, bool quad = false)
 {
     if (!workspace || !out_color || !bg_color || width <= 0 || height <= 0 || !valid_tile_shape(block_x, block_y))
         return GSR_INVALID_ARG;
+    if (quad && (block_x != 16 || block_y != 16 || variant == GSR_RENDER_SPLIT)) return GSR_INVALID_ARG;
     if (render_needs_ranges(variant) ? !ranges : (!keys_sorted && !ranges)) return GSR_INVALID_ARG;
     if (variant < 0 || variant > GSR_RENDER_SPLIT) return GSR_INVALID_ARG;
     RenderArgs a;
@@ -358,6 +386,7 @@ static gsr_status render_impl(int variant, int num, const int32_t* d_num, long l
     a.bg[2] = bg_color[2];
     a.out = out_color;
     a.ws = reinterpret_cast<WorkspaceHeader*>(workspace);
+    a.quad = quad ? 1 : 0;
     return from_cuda(launch_render(a, s));
 }
 
@@ -381,7 +410,12 @@ gsr_status gsr_forward(int variant, int P, const float* pos, const void* shs, in
                        int32_t* ranges, const float* bg_color, uint8_t* out_color, gsr_stream_t stream)
 {
     cudaStream_t s = (cudaStream_t)stream;
+    // GSR_QUAD_KEYS: one key per 2x2 group of 16x16 tiles, same image
+    const bool quad = (variant & GSR_QUAD_KEYS) != 0;
+    variant &= ~GSR_QUAD_KEYS;
     if (!workspace || !curr_offset || !valid_tile_shape(block_x, block_y)) return GSR_INVALID_ARG;
+    if (quad && (block_x != 16 || block_y != 16 || variant == GSR_RENDER_SPLIT || P > (int)kQuadGidMask))
+        return GSR_INVALID_ARG;
     if (render_needs_ranges(variant) && !ranges) return GSR_INVALID_ARG;
     if (workspace_bytes < sort_workspace_bytes(key_capacity)) return GSR_INVALID_ARG;
     profile_frame_begin();
@@ -392,10 +426,12 @@ gsr_status gsr_forward(int variant, int P, const float* pos, const void* shs, in
     gsr_status st = preprocess_impl(P, pos, shs, shs_half, opacity, cov3d, width, height, block_x, block_y, cam_pos,
                                     cam_rot, focal_x, focal_y, z_far, z_near, points_xy, rgb_depth, conic_opacity,
                                     keys_unsorted, values_unsorted, key_capacity, curr_offset, workspace,
-                                    workspace_bytes, s);
+                                    workspace_bytes, s, quad);
     if (st != GSR_OK) return st;
     profile_mark(s);
-    const int tiles = tiles_of(width, height, block_x, block_y);
+    // key tile ids: tiles, or quads
+    const int tiles = quad ? quad_cols(div_up(width, 16)) * quad_cols(div_up(height, 16))
+                           : tiles_of(width, height, block_x, block_y);
     // the preprocess recorded the depth range in the workspace header: sort
     // the (tile, depth - floor) word in as few passes as it needs
     st = sort_impl(0, curr_offset, 32 + bits_for((uint32_t)tiles), workspace, workspace_bytes, keys_unsorted,
@@ -410,7 +446,7 @@ gsr_status gsr_forward(int variant, int P, const float* pos, const void* shs, in
         profile_mark(s);
     }
     st = render_impl(variant, 0, curr_offset, key_capacity, width, height, block_x, block_y, P, points_xy, rgb_depth,
-                     conic_opacity, keys_sorted, values_sorted, ranges, bg_color, out_color, workspace, s);
+                     conic_opacity, keys_sorted, values_sorted, ranges, bg_color, out_color, workspace, s, quad);
     if (st == GSR_OK) profile_mark(s);
     return st;
 }

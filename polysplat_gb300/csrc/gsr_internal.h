@@ -30,6 +30,12 @@ struct MassiveQueue {
     uint32_t* depth_hi;  // max depth bits of emitting Gaussians (for the sort's key compression)
 };
 
+// Tile id (and value) of a pair slot that a Gaussian's emission could not
+// fill: the depth-first and ES emissions write exactly the counted number of
+// pairs per Gaussian, padding with this id, which sorts after every real tile
+// under any tile-id mask and which the tile ranges treat as past the end.
+constexpr uint32_t kTileSentinel = 0xFFFFFFFFu;
+
 // Per-Gaussian records of the depth-first pipeline's counting pass.
 struct DepthFirstRecords {
     uint32_t* count;  // [P] number of tiles the Gaussian's keys go to
@@ -70,7 +76,21 @@ struct PreprocessParams {
     // dispatch thresholds of the multi-tile emission (tiles of the rectangle)
     int massive_area;
     int huge_area;
+    // Quad keys (bx = by = 16 only): one key per 2x2 group of tiles that the
+    // Gaussian hits, with the quad's id as the key's tile id (quads numbered
+    // row-major over ceil(gx / 2) columns) and the hit tiles as a 4-bit mask
+    // in the value's top bits (see kQuadShift).
+    int quad = 0;
 };
+// Quad keys: bit (x & 1) | (y & 1) << 1 of value >> kQuadShift is set when
+// the Gaussian hits tile (x, y) of the quad, by the same exact tile test the
+// per-tile emission uses; the Gaussian's index is value & kQuadGidMask.
+// So the Gaussians listed for one tile, in key order, are exactly that tile's
+// per-tile list, while the sort handles one key per quad.
+constexpr int kQuadShift = 28;
+constexpr uint32_t kQuadGidMask = (1u << kQuadShift) - 1u;
+__host__ __device__ inline int quad_cols(int gx) { return (gx + 1) >> 1; }
+
 constexpr int kDefaultMassiveArea = 32;
 constexpr int kDefaultHugeArea = 2048;
 
@@ -226,6 +246,7 @@ struct RenderArgs {
     float bg[3];
     uint8_t* out;
     WorkspaceHeader* ws;
+    int quad = 0;  // keys and ranges per 2x2 group of 16x16 tiles (PreprocessParams::quad)
 };
 cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream);
 
@@ -254,7 +275,8 @@ struct TrainRenderArgs {
 cudaError_t launch_render_train(const TrainRenderArgs& a, bool backward, cudaStream_t stream);
 
 // One view of a batched render: its tiles are [tile_base, tile_base +
-// gx * gy) of the batch's global tile ids.
+// gx * gy) of the batch's global tile ids (quads, with gx quads per row, for
+// quad renders).
 struct RenderView {
     int tile_base;
     int gx;
@@ -279,6 +301,18 @@ cudaError_t launch_depth_first(const PreprocessParams& p, bool half_sh, void* sc
                                cudaStream_t stream);
 
 int device_sm_count();
+// Per-device host caches (occupancy, attribute set-up) hold kMaxDevices
+// entries; current_device() is the current device, or -1 when the query
+// fails or the index is beyond the caches.
+constexpr int kMaxDevices = 64;
+int current_device();
+
+// Failure-detection hooks (gsr_debug_*): the look-back spin bound the next
+// sorts use (kSpinLimit unless a test lowered it), and whether the first
+// digit pass of the next sorts leaves tile 0 untaken, so that every later
+// tile's look-back waits on an entry nobody publishes.
+uint32_t sort_wait_limit();
+bool sort_stall_first_tile();
 
 // Stage-timing hook (gsr_set_profile_events): records the next caller-owned
 // event on `stream` when profiling is on; no-op otherwise.

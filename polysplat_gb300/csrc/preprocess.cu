@@ -174,30 +174,41 @@ __device__ __forceinline__ V3 sh_color(int idx, V3 p, V3 cam, const void* shs)
 }
 
 // Ellipse / tile-box tests (preprocess.cu:257-311).
+//
+// The arithmetic is written with explicit rounding intrinsics, one per
+// operation of the reference's expressions, fused where those expressions
+// contract under fast math (x * y + z -> fma(x, y, z); x * x - y * z ->
+// fma(x, x, -(y * z))).  Left to the compiler, the fusion of the same
+// expression can differ between the kernels that inline it, and a tile on
+// the ellipse's edge then passes in one kernel and fails in another: the
+// depth-first pipeline counts a Gaussian's tiles in one kernel and emits
+// them in another, so the two must agree bit for bit.
 __device__ __forceinline__ bool seg_hits_ellipse(float a, float b, float c, float d, float l, float r)
 {
-    float delta = b * b - 4.0f * a * c;
-    float t1 = (l - d) * (2.0f * a) + b;
-    float t2 = (r - d) * (2.0f * a) + b;
-    return delta >= 0.0f && (t1 <= 0.0f || t1 * t1 <= delta) && (t2 >= 0.0f || t2 * t2 <= delta);
+    const float two_a = __fmul_rn(2.0f, a);
+    const float delta = __fmaf_rn(b, b, -__fmul_rn(__fmul_rn(4.0f, a), c));
+    const float t1 = __fmaf_rn(__fsub_rn(l, d), two_a, b);
+    const float t2 = __fmaf_rn(__fsub_rn(r, d), two_a, b);
+    return delta >= 0.0f && (t1 <= 0.0f || __fmul_rn(t1, t1) <= delta) &&
+           (t2 >= 0.0f || __fmul_rn(t2, t2) <= delta);
 }
 
 __device__ __forceinline__ bool box_hits_ellipse(int2 pmin, int2 pmax, float2 ctr, float3 con, float power)
 {
     float a, b, c, dx, dy;
-    float w = 2.0f * power;
-    if (ctr.x * 2.0f < pmin.x + pmax.x) dx = ctr.x - pmin.x;
-    else dx = ctr.x - pmax.x;
+    const float w = __fmul_rn(2.0f, power);
+    if (ctr.x * 2.0f < (float)(pmin.x + pmax.x)) dx = __fsub_rn(ctr.x, (float)pmin.x);
+    else dx = __fsub_rn(ctr.x, (float)pmax.x);
     a = con.z;
-    b = -2.0f * con.y * dx;
-    c = con.x * dx * dx - w;
-    if (seg_hits_ellipse(a, b, c, ctr.y, pmin.y, pmax.y)) return true;
-    if (ctr.y * 2.0f < pmin.y + pmax.y) dy = ctr.y - pmin.y;
-    else dy = ctr.y - pmax.y;
+    b = __fmul_rn(__fmul_rn(-2.0f, con.y), dx);
+    c = __fmaf_rn(__fmul_rn(con.x, dx), dx, -w);
+    if (seg_hits_ellipse(a, b, c, ctr.y, (float)pmin.y, (float)pmax.y)) return true;
+    if (ctr.y * 2.0f < (float)(pmin.y + pmax.y)) dy = __fsub_rn(ctr.y, (float)pmin.y);
+    else dy = __fsub_rn(ctr.y, (float)pmax.y);
     a = con.x;
-    b = -2.0f * con.y * dy;
-    c = con.z * dy * dy - w;
-    return seg_hits_ellipse(a, b, c, ctr.x, pmin.x, pmax.x);
+    b = __fmul_rn(__fmul_rn(-2.0f, con.y), dy);
+    c = __fmaf_rn(__fmul_rn(con.z, dy), dy, -w);
+    return seg_hits_ellipse(a, b, c, ctr.x, (float)pmin.x, (float)pmax.x);
 }
 
 __device__ __forceinline__ bool box_has_centre(int2 pmin, int2 pmax, float2 c)
@@ -211,6 +222,26 @@ __device__ __forceinline__ bool tile_hit(int x, int y, int bx, int by, float2 ct
     int2 pmax = {pmin.x + bx - 1, pmin.y + by - 1};
     return box_has_centre(pmin, pmax, ctr) || (power > 0.0f && box_hits_ellipse(pmin, pmax, ctr, con, power));
 }
+
+// Tiles of quad (qx, qy) that lie in the Gaussian's rectangle [rmin, rmax)
+// and pass tile_hit: bit (x & 1) | (y & 1) << 1 per hit tile.  These are
+// exactly the tiles the per-tile emission would give keys.
+__device__ __forceinline__ uint32_t quad_mask(int qx, int qy, int2 rmin, int2 rmax, int bx, int by, float2 ctr,
+                                              float3 con, float power)
+{
+    uint32_t m = 0u;
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        const int x = 2 * qx + (s & 1), y = 2 * qy + (s >> 1);
+        if (x >= rmin.x && x < rmax.x && y >= rmin.y && y < rmax.y && tile_hit(x, y, bx, by, ctr, con, power))
+            m |= 1u << s;
+    }
+    return m;
+}
+
+// Quad-rectangle [q0, q1) covering tile columns (or rows) [t0, t1), t1 > t0.
+__device__ __forceinline__ int quad_lo(int t0) { return t0 >> 1; }
+__device__ __forceinline__ int quad_hi(int t1) { return ((t1 - 1) >> 1) + 1; }
 
 // ---------------------------------------------------------------------------
 // Per-warp key staging.  A warp appends up to 32 keys per step into its own
@@ -308,9 +339,14 @@ __device__ __forceinline__ void block_flush(Stage& st, const EmitOut& out, int* 
 // pipeline).  COUNT = true: the depth-first pipeline's counting pass -- the
 // same tests, but each Gaussian's number of hit tiles is counted and written
 // with its depth and test geometry instead of keys.
-template <bool HALF, bool COUNT, bool VIEWS>
+//
+// QUAD (emission only): keys name 2x2 groups of tiles, with the hit tiles as a
+// mask in the value (PreprocessParams::quad); the tile rectangle, the dispatch
+// and every tile test are the per-tile emission's.
+template <bool HALF, bool COUNT, bool VIEWS, bool QUAD = false>
 __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __grid_constant__ PreprocessParams a0)
 {
+    static_assert(!(QUAD && COUNT), "quad keys are an emission mode");
     // VIEWS: the views' blocks follow one another along the grid (parameter
     // blocks in device memory); a block past the last view has no work
     int vi = 0, lblock = (int)blockIdx.x;
@@ -343,6 +379,7 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
     const int warp_first = idx - (int)lane;
     const int tx = lane & 7, ty = lane >> 3;  // 8x4 tile window of the massive path
     const int gridx = a.gx, gridy = a.gy;
+    const int qgx = quad_cols(gridx);  // quads per row (QUAD)
 
     bool point_valid = false;
     V3 p_orig = {0.f, 0.f, 0.f};
@@ -402,6 +439,11 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
         bool v = single && tile_hit(rect_min.x, rect_min.y, a.bx, a.by, point_xy, conic, power);
         if (COUNT) {
             if (v) s_cnt[warp][lane] = 1u;
+        } else if (QUAD) {
+            const uint32_t qt = (uint32_t)(a.tile_base + (rect_min.y >> 1) * qgx + (rect_min.x >> 1));
+            const uint32_t bit = 1u << ((rect_min.x & 1) | ((rect_min.y & 1) << 1));
+            stage_emit(st, out, v, ((uint64_t)qt << 32) | depth_bits, (uint32_t)(a.gid_base + idx) | (bit << kQuadShift),
+                       lane);
         } else {
             uint64_t key = ((uint64_t)(uint32_t)(a.tile_base + rect_min.y * gridx + rect_min.x) << 32) | depth_bits;
             stage_emit(st, out, v, key, (uint32_t)(a.gid_base + idx), lane);
@@ -466,17 +508,33 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
         const uint32_t db = __shfl_sync(GSR_FULL_MASK, depth_bits, i);
         const float pw = __shfl_sync(GSR_FULL_MASK, power, i);
         const uint32_t gid = (uint32_t)(a.gid_base + warp_first + i);
-        for (int y0 = y_lo; y0 < y_hi; y0 += 4) {
-            const int y = y0 + ty;
-            for (int x0 = x_lo; x0 < x_hi; x0 += 8) {
-                const int x = x0 + tx;
-                bool v = y < y_hi && x < x_hi && tile_hit(x, y, a.bx, a.by, c, q, pw);
-                if (COUNT) {
-                    const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
-                    if (lane == 0) s_cnt[warp][i] += __popc(m);
-                } else {
-                    uint64_t key = ((uint64_t)(uint32_t)(a.tile_base + y * gridx + x) << 32) | db;
-                    stage_emit(st, out, v, key, gid, lane);
+        if (QUAD) {
+            const int qx_lo = quad_lo(x_lo), qx_hi = quad_hi(x_hi), qy_lo = quad_lo(y_lo), qy_hi = quad_hi(y_hi);
+            for (int y0 = qy_lo; y0 < qy_hi; y0 += 4) {
+                const int qy = y0 + ty;
+                for (int x0 = qx_lo; x0 < qx_hi; x0 += 8) {
+                    const int qx = x0 + tx;
+                    const uint32_t m = (qy < qy_hi && qx < qx_hi)
+                                           ? quad_mask(qx, qy, make_int2(x_lo, y_lo), make_int2(x_hi, y_hi), a.bx,
+                                                       a.by, c, q, pw)
+                                           : 0u;
+                    const uint64_t key = ((uint64_t)(uint32_t)(a.tile_base + qy * qgx + qx) << 32) | db;
+                    stage_emit(st, out, m != 0u, key, gid | (m << kQuadShift), lane);
+                }
+            }
+        } else {
+            for (int y0 = y_lo; y0 < y_hi; y0 += 4) {
+                const int y = y0 + ty;
+                for (int x0 = x_lo; x0 < x_hi; x0 += 8) {
+                    const int x = x0 + tx;
+                    bool v = y < y_hi && x < x_hi && tile_hit(x, y, a.bx, a.by, c, q, pw);
+                    if (COUNT) {
+                        const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
+                        if (lane == 0) s_cnt[warp][i] += __popc(m);
+                    } else {
+                        uint64_t key = ((uint64_t)(uint32_t)(a.tile_base + y * gridx + x) << 32) | db;
+                        stage_emit(st, out, v, key, gid, lane);
+                    }
                 }
             }
         }
@@ -484,7 +542,11 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
     }
     point_valid = point_valid && !massive;
 
-    const int my_tiles = point_valid ? area : 0;
+    // tasks of the pool: the rectangle's tiles, or (QUAD) the quads covering it
+    const int my_tiles = !point_valid ? 0
+                         : QUAD      ? (quad_hi(rect_max.x) - quad_lo(rect_min.x)) *
+                                      (quad_hi(rect_max.y) - quad_lo(rect_min.y))
+                                     : area;
     const unsigned multi = __ballot_sync(GSR_FULL_MASK, point_valid);
     if (multi) {
         int prefix = my_tiles;
@@ -521,7 +583,19 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
             const uint32_t db = __shfl_sync(GSR_FULL_MASK, depth_bits, owner);
             int x = 0, y = 0;
             bool v = false;
-            if (task_ok) {
+            uint32_t qm = 0u;
+            if (QUAD) {
+                const int oy1 = __shfl_sync(GSR_FULL_MASK, rect_max.y, owner);
+                const int oqx = quad_lo(ox), oqw = quad_hi(ox + ow) - oqx;
+                if (task_ok) {
+                    const int local = task - op;
+                    const int row = oqw > 0 ? local / oqw : 0;
+                    x = oqx + (local - row * oqw);
+                    y = quad_lo(oy) + row;
+                    qm = quad_mask(x, y, make_int2(ox, oy), make_int2(ox + ow, oy1), a.bx, a.by, c, q, pw);
+                    v = qm != 0u;
+                }
+            } else if (task_ok) {
                 const int local = task - op;
                 const int row = ow > 0 ? local / ow : 0;
                 x = ox + (local - row * ow);
@@ -530,6 +604,9 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
             }
             if (COUNT) {
                 if (v) atomicAdd(&s_cnt[warp][owner], 1u);
+            } else if (QUAD) {
+                const uint64_t key = ((uint64_t)(uint32_t)(a.tile_base + y * qgx + x) << 32) | db;
+                stage_emit(st, out, v, key, (uint32_t)(a.gid_base + warp_first + owner) | (qm << kQuadShift), lane);
             } else {
                 uint64_t key = ((uint64_t)(uint32_t)(a.tile_base + y * gridx + x) << 32) | db;
                 stage_emit(st, out, v, key, (uint32_t)(a.gid_base + warp_first + owner), lane);
@@ -776,6 +853,146 @@ __device__ __forceinline__ void sweep_warp(const MassiveEntry& me, const Preproc
     }
 }
 
+// Candidate quad columns [q_lo, q_hi] of quad row `qy`: the union of the
+// candidate tile columns of its (one or two) tile rows inside [y_lo, y_hi).
+__device__ __forceinline__ bool band_quads(const Band& e, int qy, int by, int bx, int x_lo, int x_hi, int y_lo,
+                                           int y_hi, int& q_lo, int& q_hi)
+{
+    int lo = 0x7FFFFFFF, hi = -1;
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+        const int ty = 2 * qy + s;
+        int clo = 0, chi = -1;
+        if (ty >= y_lo && ty < y_hi && band_columns(e, ty, by, bx, x_lo, x_hi, clo, chi)) {
+            lo = min(lo, clo);
+            hi = max(hi, chi);
+        }
+    }
+    q_lo = lo >> 1;
+    q_hi = hi >> 1;
+    return hi >= lo;
+}
+
+// sweep_cta over quads: on_step(v, qx, qy, mask) with mask = quad_mask() of
+// the quad and v = mask != 0.  A tile that passes the exact test lies in its
+// row's band, so its quad lies in the quad row's band.
+template <typename F>
+__device__ __forceinline__ void sweep_cta_quad(const MassiveEntry& me, const PreprocessParams& a, short2* s_band,
+                                               unsigned lane, int warp, F&& on_step)
+{
+    const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
+    const float pw = me.ctr_power_depth.z;
+    const float3 q = {me.conic_gid.x, me.conic_gid.y, me.conic_gid.z};
+    const int x_lo = me.rect.x & 0xFFFF, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
+    const int2 rmin = make_int2(x_lo, y_lo), rmax = make_int2(x_hi, y_hi);
+    const int qx_lo = quad_lo(x_lo), qx_hi = quad_hi(x_hi), qy_lo = quad_lo(y_lo), qy_hi = quad_hi(y_hi);
+    const Band eb = make_band(q, pw, c);
+    if (eb.ok && (qy_hi - qy_lo) <= kMaxBandRows) {
+        for (int r = threadIdx.x; r < qy_hi - qy_lo; r += kThreads) {
+            int lo = 0, hi = -1;
+            if (!band_quads(eb, qy_lo + r, a.by, a.bx, x_lo, x_hi, y_lo, y_hi, lo, hi)) {
+                lo = 0;
+                hi = -1;
+            }
+            s_band[r] = make_short2((short)lo, (short)hi);
+        }
+        __syncthreads();
+        for (int r = warp; r < qy_hi - qy_lo; r += kWarps) {
+            const short2 band = s_band[r];
+            const int qy = qy_lo + r;
+            for (int x0 = band.x; x0 <= band.y; x0 += 32) {
+                const int qx = x0 + (int)lane;
+                const uint32_t m = qx <= band.y ? quad_mask(qx, qy, rmin, rmax, a.bx, a.by, c, q, pw) : 0u;
+                on_step(m != 0u, qx, qy, m);
+            }
+        }
+        __syncthreads();
+        return;
+    }
+    // windows of (cols x rows) quads, as sweep_cta does for tiles
+    const int w = qx_hi - qx_lo;
+    int lg = 5;
+    while (lg > 0 && (1 << (lg - 1)) >= w) lg--;
+    const int cols = 1 << lg;
+    const int rows_w = 32 >> lg;
+    const int rows_cta = rows_w * kWarps;
+    const int lx = (int)lane & (cols - 1);
+    const int ly = warp * rows_w + ((int)lane >> lg);
+    for (int wy = qy_lo; wy < qy_hi; wy += rows_cta) {
+        const int qy = wy + ly;
+        for (int wx = qx_lo; wx < qx_hi; wx += cols) {
+            const int qx = wx + lx;
+            const uint32_t m =
+                (qy < qy_hi && qx < qx_hi) ? quad_mask(qx, qy, rmin, rmax, a.bx, a.by, c, q, pw) : 0u;
+            on_step(m != 0u, qx, qy, m);
+        }
+    }
+    __syncthreads();
+}
+
+// sweep_warp over quads (see sweep_cta_quad).
+template <typename F>
+__device__ __forceinline__ void sweep_warp_quad(const MassiveEntry& me, const PreprocessParams& a, unsigned lane,
+                                                F&& on_step)
+{
+    const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
+    const float pw = me.ctr_power_depth.z;
+    const float3 q = {me.conic_gid.x, me.conic_gid.y, me.conic_gid.z};
+    const int x_lo = me.rect.x & 0xFFFF, x_hi = me.rect.y, y_lo = me.rect.z, y_hi = me.rect.w;
+    const int2 rmin = make_int2(x_lo, y_lo), rmax = make_int2(x_hi, y_hi);
+    const int qx_lo = quad_lo(x_lo), qx_hi = quad_hi(x_hi), qy_lo = quad_lo(y_lo), qy_hi = quad_hi(y_hi);
+    const Band eb = make_band(q, pw, c);
+    if (eb.ok) {
+        for (int r0 = qy_lo; r0 < qy_hi; r0 += 32) {
+            const int qy = r0 + (int)lane;
+            int clo = 0, n = 0;
+            if (qy < qy_hi) {
+                int chi = -1;
+                if (band_quads(eb, qy, a.by, a.bx, x_lo, x_hi, y_lo, y_hi, clo, chi)) n = chi - clo + 1;
+            }
+            int pref = n;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int t = __shfl_up_sync(GSR_FULL_MASK, pref, d);
+                if ((int)lane >= d) pref += t;
+            }
+            const int total = __shfl_sync(GSR_FULL_MASK, pref, 31);
+            for (int base = 0; base < total; base += 32) {
+                const int task = base + (int)lane;
+                int lo = 0, hi = 31;
+#pragma unroll
+                for (int step = 0; step < 5; step++) {
+                    const int mid = (lo + hi) >> 1;
+                    if (__shfl_sync(GSR_FULL_MASK, pref, mid) > task) hi = mid;
+                    else lo = mid + 1;
+                }
+                const int o_pref = __shfl_sync(GSR_FULL_MASK, pref, lo);
+                const int o_n = __shfl_sync(GSR_FULL_MASK, n, lo);
+                const int o_clo = __shfl_sync(GSR_FULL_MASK, clo, lo);
+                const int qx = o_clo + task - (o_pref - o_n);
+                const int qyy = r0 + lo;
+                const uint32_t m = task < total ? quad_mask(qx, qyy, rmin, rmax, a.bx, a.by, c, q, pw) : 0u;
+                on_step(m != 0u, qx, qyy, m);
+            }
+        }
+        return;
+    }
+    const int w = qx_hi - qx_lo;
+    const long long total = (long long)w * (long long)(qy_hi - qy_lo);
+    for (long long base = 0; base < total; base += 32) {
+        const long long t = base + lane;
+        int qx = 0, qy = 0;
+        uint32_t m = 0u;
+        if (t < total) {
+            const int r = (int)(t / w);
+            qy = qy_lo + r;
+            qx = qx_lo + (int)(t - (long long)r * w);
+            m = quad_mask(qx, qy, rmin, rmax, a.bx, a.by, c, q, pw);
+        }
+        on_step(m != 0u, qx, qy, m);
+    }
+}
+
 // Where the depth-first pipeline's emission pass writes a queued Gaussian.
 struct DfEmit {
     const uint32_t* offsets;  // [V] first output position of the s-th Gaussian in depth order
@@ -791,9 +1008,10 @@ enum : int { kMassiveEmit64 = 0, kMassiveCount = 1, kMassiveEmitDf = 2 };
 // time with all 256 threads, then each warp takes large rectangles on its
 // own.  MODE: emit 64-bit keys, count the hit tiles (depth-first counting
 // pass), or write depth-first pairs at the Gaussian's offset.
-template <int MODE, bool VIEWS>
+template <int MODE, bool VIEWS, bool QUAD = false>
 __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant__ PreprocessParams a, const DfEmit df)
 {
+    static_assert(!QUAD || MODE == kMassiveEmit64, "quad keys are an emission mode");
     __shared__ uint64_t s_keys[MODE == kMassiveEmit64 ? kWarps : 1][kStage];
     __shared__ uint32_t s_vals[MODE == kMassiveEmit64 ? kWarps : 1][kStage];
     __shared__ int s_fill[kWarps];
@@ -825,7 +1043,13 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
         const uint32_t gid = __float_as_uint(me.conic_gid.w);
         if (VIEWS && ((uint32_t)me.rect.x >> 16) >= (uint32_t)a.n_views) continue;
         const PreprocessParams& av = VIEWS ? a.views[(uint32_t)me.rect.x >> 16] : a;
-        if (MODE == kMassiveEmit64) {
+        if (MODE == kMassiveEmit64 && QUAD) {
+            const int qgx = quad_cols(av.gx);
+            sweep_cta_quad(me, av, s_band, lane, warp, [&](bool v, int qx, int qy, uint32_t m) {
+                uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + qy * qgx + qx) << 32) | db;
+                stage_emit(st, out, v, key, gid | (m << kQuadShift), lane);
+            });
+        } else if (MODE == kMassiveEmit64) {
             sweep_cta(me, av, s_band, lane, warp, [&](bool v, int x, int y) {
                 uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + y * av.gx + x) << 32) | db;
                 stage_emit(st, out, v, key, gid, lane);
@@ -844,7 +1068,8 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
             }
         } else {
             // Gaussians that hit no tile were not ranked
-            if (a.df.count[gid] == 0u) continue;
+            const uint32_t count = a.df.count[gid];
+            if (count == 0u) continue;
             const long long base = df.offsets[df.rank[gid]];
             sweep_cta(me, a, s_band, lane, warp, [&](bool v, int x, int y) {
                 const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
@@ -852,14 +1077,21 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
                 uint32_t w0 = 0;
                 if (lane == 0) w0 = atomicAdd(&s_pos, (uint32_t)__popc(m));
                 w0 = __shfl_sync(GSR_FULL_MASK, w0, 0);
-                if (v) {
-                    const long long pos = base + w0 + __popc(m & lanemask_lt());
-                    if (pos < df.cap) {
-                        df.tiles[pos] = (uint32_t)(y * a.gx + x);
-                        df.vals[pos] = gid;
-                    }
+                const uint32_t k = w0 + __popc(m & lanemask_lt());
+                if (v && k < count && base + k < df.cap) {  // never past the Gaussian's own slots
+                    df.tiles[base + k] = (uint32_t)(y * a.gx + x);
+                    df.vals[base + k] = gid;
                 }
             });
+            // sweep_cta ended on a barrier, so s_pos is final; every thread
+            // reads it before thread 0 resets it for the next entry
+            const uint32_t filled = s_pos;
+            __syncthreads();
+            for (uint32_t k = filled + threadIdx.x; k < count; k += kThreads)  // pad unfilled slots
+                if (base + k < df.cap) {
+                    df.tiles[base + k] = kTileSentinel;
+                    df.vals[base + k] = kTileSentinel;
+                }
         }
     }
 
@@ -874,7 +1106,13 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
         const uint32_t gid = __float_as_uint(me.conic_gid.w);
         if (VIEWS && ((uint32_t)me.rect.x >> 16) >= (uint32_t)a.n_views) continue;
         const PreprocessParams& av = VIEWS ? a.views[(uint32_t)me.rect.x >> 16] : a;
-        if (MODE == kMassiveEmit64) {
+        if (MODE == kMassiveEmit64 && QUAD) {
+            const int qgx = quad_cols(av.gx);
+            sweep_warp_quad(me, av, lane, [&](bool v, int qx, int qy, uint32_t m) {
+                uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + qy * qgx + qx) << 32) | db;
+                stage_emit(st, out, v, key, gid | (m << kQuadShift), lane);
+            });
+        } else if (MODE == kMassiveEmit64) {
             sweep_warp(me, av, lane, [&](bool v, int x, int y) {
                 uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + y * av.gx + x) << 32) | db;
                 stage_emit(st, out, v, key, gid, lane);
@@ -884,20 +1122,24 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
             sweep_warp(me, a, lane, [&](bool v, int, int) { cnt += __popc(__ballot_sync(GSR_FULL_MASK, v)); });
             if (lane == 0) a.df.count[gid] = cnt;
         } else {
-            if (a.df.count[gid] == 0u) continue;
+            const uint32_t count = a.df.count[gid];
+            if (count == 0u) continue;
             const long long base = df.offsets[df.rank[gid]];
             uint32_t wpos = 0;
             sweep_warp(me, a, lane, [&](bool v, int x, int y) {
                 const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
-                if (v) {
-                    const long long pos = base + wpos + __popc(m & lanemask_lt());
-                    if (pos < df.cap) {
-                        df.tiles[pos] = (uint32_t)(y * a.gx + x);
-                        df.vals[pos] = gid;
-                    }
+                const uint32_t k = wpos + __popc(m & lanemask_lt());
+                if (v && k < count && base + k < df.cap) {
+                    df.tiles[base + k] = (uint32_t)(y * a.gx + x);
+                    df.vals[base + k] = gid;
                 }
                 wpos += __popc(m);
             });
+            for (uint32_t k = wpos + lane; k < count; k += 32)
+                if (base + k < df.cap) {
+                    df.tiles[base + k] = kTileSentinel;
+                    df.vals[base + k] = kTileSentinel;
+                }
         }
     }
     if (MODE == kMassiveEmit64) block_flush(st, out, s_fill, s_base, lane, warp);
@@ -922,14 +1164,20 @@ __global__ __launch_bounds__(256) void k_df_emit_small(const PreprocessParams a,
         const float2 ctr = __ldg(a.points_xy + gid);
         const float3 con = {g.x, g.y, g.z};
         long long pos = __ldg(df.offsets + s);
+        const long long lim = pos + __ldg(a.df.count + gid);  // the Gaussian's own slots
         for (int y = y0; y < y1; y++)
             for (int x = x0; x < x1; x++) {
                 if (!tile_hit(x, y, a.bx, a.by, ctr, con, g.w)) continue;
-                if (pos < df.cap) {
+                if (pos < lim && pos < df.cap) {
                     df.tiles[pos] = (uint32_t)(y * a.gx + x);
                     df.vals[pos] = gid;
                 }
                 pos++;
+            }
+        for (; pos < lim; pos++)  // pad unfilled slots
+            if (pos < df.cap) {
+                df.tiles[pos] = kTileSentinel;
+                df.vals[pos] = kTileSentinel;
             }
     }
 }
@@ -1040,10 +1288,14 @@ static cudaError_t preprocess_common(const PreprocessParams& p, bool half_sh, bo
         cudaError_t e = cudaMemsetAsync(p.mq.count, 0, kPreprocessRegionBytes, stream);
         if (e != cudaSuccess) return e;
     }
+    if (p.quad && (count || p.bx != 16 || p.by != 16)) return cudaErrorInvalidValue;
     const int grid = div_up(p.P, kThreads);
     if (count) {
         if (half_sh) k_preprocess<true, true, false><<<grid, kThreads, 0, stream>>>(p);
         else k_preprocess<false, true, false><<<grid, kThreads, 0, stream>>>(p);
+    } else if (p.quad) {
+        if (half_sh) k_preprocess<true, false, false, true><<<grid, kThreads, 0, stream>>>(p);
+        else k_preprocess<false, false, false, true><<<grid, kThreads, 0, stream>>>(p);
     } else {
         if (half_sh) k_preprocess<true, false, false><<<grid, kThreads, 0, stream>>>(p);
         else k_preprocess<false, false, false><<<grid, kThreads, 0, stream>>>(p);
@@ -1052,6 +1304,9 @@ static cudaError_t preprocess_common(const PreprocessParams& p, bool half_sh, bo
     if (e != cudaSuccess || p.mq.capacity <= 0) return e;
     const DfEmit none{nullptr, nullptr, nullptr, nullptr, 0};
     if (count) k_emit_massive<kMassiveCount, false><<<emit_grid(k_emit_massive<kMassiveCount, false>), kThreads, 0, stream>>>(p, none);
+    else if (p.quad)
+        k_emit_massive<kMassiveEmit64, false, true>
+            <<<emit_grid(k_emit_massive<kMassiveEmit64, false, true>), kThreads, 0, stream>>>(p, none);
     else k_emit_massive<kMassiveEmit64, false><<<emit_grid(k_emit_massive<kMassiveEmit64, false>), kThreads, 0, stream>>>(p, none);
     return cudaGetLastError();
 }
@@ -1061,13 +1316,23 @@ cudaError_t launch_preprocess_views(const PreprocessParams& base, int n_views, i
 {
     if (n_views <= 0 || blocks <= 0) return cudaSuccess;
     if (n_views > 32767 || !base.views || base.mq.capacity <= 0) return cudaErrorInvalidValue;
+    if (base.quad && (base.bx != 16 || base.by != 16)) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(base.mq.count, 0, kPreprocessRegionBytes, stream);
     if (e != cudaSuccess) return e;
     const dim3 grid(blocks);
+    const DfEmit none{nullptr, nullptr, nullptr, nullptr, 0};
+    if (base.quad) {
+        // every view's block carries the same quad flag as the base block
+        if (half_sh) k_preprocess<true, false, true, true><<<grid, kThreads, 0, stream>>>(base);
+        else k_preprocess<false, false, true, true><<<grid, kThreads, 0, stream>>>(base);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        k_emit_massive<kMassiveEmit64, true, true>
+            <<<emit_grid(k_emit_massive<kMassiveEmit64, true, true>), kThreads, 0, stream>>>(base, none);
+        return cudaGetLastError();
+    }
     if (half_sh) k_preprocess<true, false, true><<<grid, kThreads, 0, stream>>>(base);
     else k_preprocess<false, false, true><<<grid, kThreads, 0, stream>>>(base);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    const DfEmit none{nullptr, nullptr, nullptr, nullptr, 0};
     k_emit_massive<kMassiveEmit64, true><<<emit_grid(k_emit_massive<kMassiveEmit64, true>), kThreads, 0, stream>>>(base, none);
     return cudaGetLastError();
 }
@@ -1138,6 +1403,11 @@ __global__ __launch_bounds__(256) void k_es_pass_b(int P, int bx, int by, int gx
             }
             wpos += __popc(m);
         });
+        for (uint32_t k = wpos + lane; k < (uint32_t)c; k += 32)  // pad unfilled slots
+            if (base + k >= 0 && base + k < cap) {
+                tiles[base + k] = kTileSentinel;
+                vals[base + k] = kTileSentinel;
+            }
     }
 }
 

@@ -44,7 +44,8 @@ struct RenderParams {
     int n_host;
     const int32_t* d_num;
     long long cap;
-    int W, H, gx, tiles, P;
+    int W, H, gx, tiles, P;  // quad renders: gx and tiles count quads
+    int items;               // work items: tiles, or 4 per quad
     const float2* xy;
     const float4* rgbd;
     const float4* con;
@@ -107,10 +108,12 @@ __device__ __forceinline__ int warp_bound(const uint64_t* __restrict__ keys, int
     return lo + __popc(__ballot_sync(GSR_FULL_MASK, pred));
 }
 
-// Stage Gaussians vals[pos, pos+cnt) into ring half `b`.
-template <bool TMA>
-__device__ __forceinline__ void stage_batch(WarpRing& R, int b, const RenderParams& p, int pos, int cnt,
-                                            unsigned lane, bool& bad)
+// Stage Gaussians vals[pos, pos+cnt) into ring half `b`; returns how many
+// were staged.  QUAD: only the values with bit `sub_bit` set (the Gaussians
+// of this warp's tile of the quad) are staged, packed to the front.
+template <bool TMA, bool QUAD = false>
+__device__ __forceinline__ int stage_batch(WarpRing& R, int b, const RenderParams& p, int pos, int cnt,
+                                           unsigned lane, bool& bad, uint32_t sub_bit = 0u)
 {
     __syncwarp();
     if (TMA) fence_proxy_async_smem();
@@ -118,10 +121,27 @@ __device__ __forceinline__ void stage_batch(WarpRing& R, int b, const RenderPara
     bool ok = (int)lane < cnt;
     if (ok) {
         gid = __ldg(p.vals + pos + lane);
-        if (gid >= (uint32_t)p.P) {  // index outside the feature arrays: skip it
+        if (QUAD) {
+            ok = (gid & sub_bit) != 0u;
+            gid &= kQuadGidMask;
+        }
+        if (ok && gid >= (uint32_t)p.P) {  // index outside the feature arrays: skip it
             ok = false;
             bad = true;
         }
+    }
+    if (QUAD) {
+        static_assert(!QUAD || !TMA, "quad renders stage with cp.async");
+        const unsigned keep = __ballot_sync(GSR_FULL_MASK, ok);
+        if (ok) {
+            const int slot = __popc(keep & lanemask_lt());
+            cp_async_16(&R.con[b][slot], p.con + gid);
+            cp_async_16(&R.rgbd[b][slot], p.rgbd + gid);
+            cp_async_8(&R.xy2[b][slot], p.xy + gid);
+            R.sel[b][slot] = 0u;
+        }
+        cp_async_commit();
+        return __popc(keep);
     }
     const bool pair_ok = ok && (gid | 1u) < (uint32_t)p.P;
     if (TMA) {
@@ -160,6 +180,7 @@ __device__ __forceinline__ void stage_batch(WarpRing& R, int b, const RenderPara
         }
         cp_async_commit();
     }
+    return cnt;
 }
 
 // Wait until ring half `b` is filled.  Returns false on timeout.
@@ -233,9 +254,15 @@ __device__ __forceinline__ void shade(float (&C)[TY][TX][3], float (&T)[TY][TX],
 // and bottom halves (8 rows each, lanes 0-15 and 16-31) stop independently,
 // as the reference's two-warp split kernels do (renderCUDAWarpSplit,
 // render.cu:4115-4357; renderCUDA32x16Split, render.cu:3859-4106).
-template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA, bool BATCH, int EXIT = 0>
+// QUAD: the keys name 2x2 groups of 16x16 tiles (ranges and key ids count
+// quads); each of a quad's four tiles is a work item of its own, whose warp
+// blends, in list order, only the Gaussians whose value has that tile's bit,
+// which is exactly the tile's per-tile list; the exit count runs over them.
+template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA, bool BATCH, int EXIT = 0,
+          bool QUAD = false>
 __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams p)
 {
+    static_assert(!QUAD || (BX == 16 && BY == 16 && EXIT == 0 && !TMA), "quad renders: 16x16 tiles");
     constexpr int TX = BX / 8, TY = BY / 4;
     __shared__ WarpRing rings[kRenderWarps];
     const unsigned lane = threadIdx.x & 31u;
@@ -257,8 +284,10 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
     bool bad = false;
     bool timed_out = false;
 
-    int tile = blockIdx.x * kRenderWarps + warp;
-    while (tile < p.tiles) {
+    int item = blockIdx.x * kRenderWarps + warp;
+    while (item < p.items) {
+        const int tile = QUAD ? (item >> 2) : item;  // key tile id (a quad's id for QUAD)
+        const int sub = item & 3;                     // QUAD: which tile of the quad
         // per-view geometry (batched renders); the single-view kernel reads
         // its parameters directly
         int W = 0, H = 0, gx = p.gx, ltile = tile;
@@ -280,8 +309,16 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
             bg = make_float3(v.bg[0], v.bg[1], v.bg[2]);
             out = reinterpret_cast<uchar3*>(v.out);
         }
-        const int ox = (ltile % gx) * BX;
-        const int oy = (ltile / gx) * BY;
+        const int ox = QUAD ? (ltile % gx) * 32 + (sub & 1) * 16 : (ltile % gx) * BX;
+        const int oy = QUAD ? (ltile / gx) * 32 + (sub >> 1) * 16 : (ltile / gx) * BY;
+        if (QUAD && (ox >= (BATCH ? W : p.W) || oy >= (BATCH ? H : p.H))) {
+            // a quad's tile beyond the image edge has no pixels and no Gaussians
+            int next = 0;
+            if (lane == 0) next = (int)atomicAdd(p.queue, 1u) + (int)gridDim.x * kRenderWarps;
+            item = __shfl_sync(GSR_FULL_MASK, next, 0);
+            continue;
+        }
+        const uint32_t sub_bit = QUAD ? (1u << (kQuadShift + sub)) : 0u;
         int start, end;
         if (RANGE_MODE == 0) {
             int2 r = make_int2(0, 0);
@@ -303,20 +340,22 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
                 C[i][j][0] = C[i][j][1] = C[i][j][2] = 0.0f;
             }
         const int total = end - start;
+        bool blended_any = false;  // QUAD: the tile's own list is not empty
         if (total > 0) {
             int cur = 0;
-            stage_batch<TMA>(R, 0, p, start, min(kBatch, total), lane, bad);
+            int staged = stage_batch<TMA, QUAD>(R, 0, p, start, min(kBatch, total), lane, bad, sub_bit);
             int processed = 0;
             bool half_done = false;  // EXIT 1: this lane's half has stopped
             for (int pos = start; pos < end; pos += kBatch) {
-                const int bsize = min(kBatch, end - pos);
+                const int bsize = staged;
                 const int npos = pos + kBatch;
                 const int nsize = max(0, min(kBatch, end - npos));
                 if (!wait_batch<TMA>(R, cur, phase_bits)) {
                     timed_out = true;
                     break;
                 }
-                if (nsize > 0) stage_batch<TMA>(R, cur ^ 1, p, npos, nsize, lane, bad);
+                if (nsize > 0) staged = stage_batch<TMA, QUAD>(R, cur ^ 1, p, npos, nsize, lane, bad, sub_bit);
+                blended_any = blended_any || bsize > 0;
                 bool exit_now = false;
                 for (int g = 0; g < bsize; g++) {
                     const float4 co = R.con[cur][g];
@@ -362,15 +401,16 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
 #pragma unroll
             for (int j = 0; j < TX; j++) {
                 const int px = ox + cb + j, py = oy + rb + i;
+                const bool any = QUAD ? blended_any : total > 0;
                 if (BATCH) {
-                    if (px < W && py < H) out[(size_t)py * W + px] = encode_px(C[i][j], T[i][j], total > 0, bg);
+                    if (px < W && py < H) out[(size_t)py * W + px] = encode_px(C[i][j], T[i][j], any, bg);
                 } else {
-                    if (px < p.W && py < p.H) p.out[(size_t)py * p.W + px] = encode_px(C[i][j], T[i][j], total > 0, p.bg);
+                    if (px < p.W && py < p.H) p.out[(size_t)py * p.W + px] = encode_px(C[i][j], T[i][j], any, p.bg);
                 }
             }
         int next = 0;
         if (lane == 0) next = (int)atomicAdd(p.queue, 1u) + (int)gridDim.x * kRenderWarps;
-        tile = __shfl_sync(GSR_FULL_MASK, next, 0);
+        item = __shfl_sync(GSR_FULL_MASK, next, 0);
     }
     if (timed_out && lane == 0) record_error(p.status, kErrTimeout);
     if (__any_sync(GSR_FULL_MASK, bad) && lane == 0) record_error(p.status, kErrBadInput);
@@ -382,19 +422,22 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
 }
 
 template <int BX, int BY, int CADENCE, int SHADER, bool DT, int RANGE_MODE, bool TMA, bool BATCH = false,
-          int EXIT = 0>
+          int EXIT = 0, bool QUAD = false>
 cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
 {
-    auto kern = k_render<BX, BY, CADENCE, SHADER, DT, RANGE_MODE, TMA, BATCH, EXIT>;
-    static std::atomic<int> per_sm_cache{0};  // host threads may race to fill it with the same value
-    int per_sm = per_sm_cache.load(std::memory_order_relaxed);
+    auto kern = k_render<BX, BY, CADENCE, SHADER, DT, RANGE_MODE, TMA, BATCH, EXIT, QUAD>;
+    // per device; host threads may race to fill it with the same value
+    static std::atomic<int> per_sm_cache[kMaxDevices];
+    const int dev = current_device();
+    if (dev < 0) return cudaErrorInvalidDevice;
+    int per_sm = per_sm_cache[dev].load(std::memory_order_relaxed);
     if (per_sm == 0) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kRenderWarps * 32, 0) != cudaSuccess ||
             per_sm < 1)
             per_sm = 1;
-        per_sm_cache.store(per_sm, std::memory_order_relaxed);
+        per_sm_cache[dev].store(per_sm, std::memory_order_relaxed);
     }
-    const int warps_needed = p.tiles;
+    const int warps_needed = p.items;
     int grid = device_sm_count() * per_sm;
     grid = max(1, min(grid, div_up(warps_needed, kRenderWarps)));
     kern<<<grid, kRenderWarps * 32, 0, stream>>>(p);
@@ -436,6 +479,25 @@ cudaError_t dispatch_shape(int variant, bool tma, const RenderParams& p, cudaStr
         return launch_variant<BX, BY, 2, 0, false, 1, false, false, 1>(p, stream);
     default:
         return cudaErrorInvalidValue;
+    }
+}
+
+// Quad renders (16x16 tiles, keys per 2x2 group of tiles; cp.async staging).
+template <bool BATCH>
+cudaError_t dispatch_quad(int variant, const RenderParams& p, cudaStream_t stream)
+{
+    const bool ranges = p.ranges != nullptr;
+    switch (variant) {
+    case GSR_RENDER_PERSISTENT_RANGES: return launch_variant<16, 16, 8, 0, false, 0, false, BATCH, 0, true>(p, stream);
+    case GSR_RENDER_PERSISTENT_FUSED:
+        if (ranges || BATCH) return launch_variant<16, 16, 16, 0, false, 0, false, BATCH, 0, true>(p, stream);
+        return launch_variant<16, 16, 16, 0, false, 1, false, false, 0, true>(p, stream);
+    case GSR_RENDER_DEFAULT:
+        if (ranges || BATCH) return launch_variant<16, 16, 2, 0, false, 0, false, BATCH, 0, true>(p, stream);
+        return launch_variant<16, 16, 2, 0, false, 1, false, false, 0, true>(p, stream);
+    case GSR_RENDER_RANGES_CADENCE2: return launch_variant<16, 16, 2, 0, false, 0, false, BATCH, 0, true>(p, stream);
+    case GSR_RENDER_DT: return launch_variant<16, 16, 8, 0, true, 0, false, BATCH, 0, true>(p, stream);
+    default: return cudaErrorInvalidValue;
     }
 }
 
@@ -710,8 +772,16 @@ cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream)
     p.cap = a.d_num ? a.cap : (long long)a.num;
     p.W = a.W;
     p.H = a.H;
-    p.gx = div_up(a.W, a.bx);
-    p.tiles = p.gx * div_up(a.H, a.by);
+    if (a.quad) {
+        if (a.bx != 16 || a.by != 16) return cudaErrorInvalidValue;
+        p.gx = quad_cols(div_up(a.W, 16));
+        p.tiles = p.gx * quad_cols(div_up(a.H, 16));
+        p.items = 4 * p.tiles;
+    } else {
+        p.gx = div_up(a.W, a.bx);
+        p.tiles = p.gx * div_up(a.H, a.by);
+        p.items = p.tiles;
+    }
     p.P = a.P;
     p.xy = a.xy;
     p.rgbd = a.rgbd;
@@ -738,6 +808,7 @@ cudaError_t launch_render_views(const RenderArgs& a, const RenderView* views_dev
     p.cap = a.d_num ? a.cap : (long long)a.num;
     p.W = p.H = p.gx = 1;  // per view
     p.tiles = total_tiles;
+    p.items = a.quad ? 4 * total_tiles : total_tiles;
     p.P = a.P;
     p.xy = a.xy;
     p.rgbd = a.rgbd;
@@ -767,11 +838,13 @@ static cudaError_t launch_prepared(const RenderArgs& a, RenderParams& p, cudaStr
         if (!p.ranges || ((reinterpret_cast<uintptr_t>(a.xy) | reinterpret_cast<uintptr_t>(a.rgbd) |
                            reinterpret_cast<uintptr_t>(a.con)) & 15u) != 0)
             return cudaErrorInvalidValue;
+        if (a.quad) return a.bx == 16 && a.by == 16 ? dispatch_quad<true>(a.variant, p, stream) : cudaErrorInvalidValue;
         if (a.bx == 16 && a.by == 16) return dispatch_batch<16, 16>(a.variant, p, stream);
         if (a.bx == 32 && a.by == 16) return dispatch_batch<32, 16>(a.variant, p, stream);
         if (a.bx == 32 && a.by == 32) return dispatch_batch<32, 32>(a.variant, p, stream);
         return cudaErrorInvalidValue;
     }
+    if (a.quad) return a.bx == 16 && a.by == 16 ? dispatch_quad<false>(a.variant, p, stream) : cudaErrorInvalidValue;
     if (a.bx == 16 && a.by == 16) return dispatch_shape<16, 16>(a.variant, tma, p, stream);
     if (a.bx == 32 && a.by == 16) return dispatch_shape<32, 16>(a.variant, tma, p, stream);
     if (a.bx == 24 && a.by == 16) return dispatch_shape<24, 16>(a.variant, tma, p, stream);

@@ -53,6 +53,7 @@ struct SortJob {
     K* keys_out;
     uint32_t* vals_out;
     SortScratch s;
+    uint32_t spin_limit;  // look-back spin bound (sort_wait_limit() at launch)
 };
 
 template <typename K>
@@ -373,7 +374,7 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortJob<K> a, int pass
                     if ((v[k] & kFlagPrefix) || j < 0) done = true;
                 }
                 if (!done && (v[0] & ~kValueMask) == 0u) {
-                    if (++spins > kSpinLimit) {
+                    if (++spins > a.spin_limit) {
                         record_error(&hdr->status, kErrTimeout);
                         break;
                     }
@@ -428,13 +429,19 @@ int sort_rank_mode()
 }
 
 template <typename K>
-cudaError_t run_sort(const SortJob<K>& a, int max_passes, cudaStream_t stream)
+cudaError_t run_sort(const SortJob<K>& job, int max_passes, cudaStream_t stream)
 {
-    if (a.cap >= (1LL << 30) || max_passes < 1 || max_passes > kMaxPasses) return cudaErrorInvalidValue;
+    if (job.cap >= (1LL << 30) || max_passes < 1 || max_passes > kMaxPasses) return cudaErrorInvalidValue;
+    SortJob<K> a = job;
+    a.spin_limit = sort_wait_limit();
     // clear the sort region of the header (pass counters and histograms)
     cudaError_t e = cudaMemsetAsync(reinterpret_cast<char*>(a.s.hdr) + kSortRegionOffset, 0,
                                     sizeof(WorkspaceHeader) - kSortRegionOffset, stream);
     if (e != cudaSuccess) return e;
+    // failure-detection hook: the first pass starts at tile 1, so tile 0 never
+    // publishes and the look-back of the tiles after it runs out
+    if (sort_stall_first_tile() && (e = cudaMemsetAsync(&a.s.hdr->pass_counter[0], 1, 1, stream)) != cudaSuccess)
+        return e;
     const int sms = device_sm_count();
     int up_grid = (int)std::min<long long>((long long)sms * 4, std::max<long long>(1, (a.cap + 2047) / 2048));
     k_upsweep<K><<<up_grid, 256, 0, stream>>>(a);
@@ -449,17 +456,21 @@ cudaError_t run_sort(const SortJob<K>& a, int max_passes, cudaStream_t stream)
     const int forced = sort_rank_mode();
     const int mode = forced != 2 ? forced : (mixed ? 2 : 1);
     auto kern = mode == 0 ? k_pass<K, 0> : mode == 1 ? k_pass<K, 1> : k_pass<K, 2>;
-    // per ranking mode: the shared-memory attribute, then the occupancy; host
-    // threads may race to fill these with the same values
-    static std::atomic<int> per_sm_cache[3];
+    // per device and ranking mode: the shared-memory attribute (a property of
+    // the kernel on each device), then the occupancy; host threads may race
+    // to fill these with the same values
+    static std::atomic<int> per_sm_cache[kMaxDevices][3];
+    const int dev = current_device();
+    if (dev < 0) return cudaErrorInvalidDevice;
     const int smem = (int)sizeof(PassSmem<K>);
-    int per_sm = per_sm_cache[mode].load(std::memory_order_acquire);
+    int per_sm = per_sm_cache[dev][mode].load(std::memory_order_acquire);
     if (per_sm == 0) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+            return e;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSortThreads, smem) != cudaSuccess ||
             per_sm < 1)
             per_sm = 1;
-        per_sm_cache[mode].store(per_sm, std::memory_order_release);
+        per_sm_cache[dev][mode].store(per_sm, std::memory_order_release);
     }
     const int grid = (int)std::min<long long>((long long)sms * per_sm, std::max<long long>(1, a.s.tiles_cap));
     for (int p = 0; p < max_passes; p++) {
@@ -547,6 +558,7 @@ cudaError_t launch_sort(const SortArgs& a, cudaStream_t stream)
     j.keys_out = a.keys_out;
     j.vals_out = a.vals_out;
     j.s = workspace_sort_scratch(a.ws, a.cap);
+    j.spin_limit = kSpinLimit;
     return run_sort(j, (a.end_bit + 7) / 8, stream);
 }
 
@@ -564,6 +576,7 @@ cudaError_t launch_sort32(int num, const int32_t* d_num, long long cap, OrderMap
     j.keys_out = keys_out;
     j.vals_out = vals_out;
     j.s = s;
+    j.spin_limit = kSpinLimit;
     return run_sort(j, max_passes, stream);
 }
 
@@ -581,6 +594,7 @@ cudaError_t launch_sort64(int num, const int32_t* d_num, long long cap, OrderMap
     j.keys_out = keys_out;
     j.vals_out = vals_out;
     j.s = s;
+    j.spin_limit = kSpinLimit;
     return run_sort(j, max_passes, stream);
 }
 

@@ -8,7 +8,13 @@
 // This entry sorts up to kStaticSortKeys pairs in a file-scope device array
 // instead.  That array is shared by every call in the process, so calls that
 // overlap in time (on different streams or from different host threads) race
-// on it and must be serialised by the caller.
+// on it and must be serialised by the caller.  A bounded wait that runs out
+// inside such a sort is recorded in the array's status word, which
+// gsr_sort_bits_static_status() reads back.
+//
+// The array's device address is looked up once per device and kept for the
+// life of the process; after cudaDeviceReset() on a device this entry point
+// must not be called on that device again.
 #include <mutex>
 
 #include "gsr_internal.h"
@@ -27,7 +33,6 @@ constexpr size_t kStaticScratchBytes = kHeaderBytes + align256s((size_t)kStaticS
 
 __device__ __align__(256) unsigned char g_static_sort_scratch[kStaticScratchBytes];
 
-constexpr int kMaxDevices = 64;
 void* g_scratch_ptr[kMaxDevices] = {};
 std::mutex g_scratch_mu;
 
@@ -35,14 +40,12 @@ std::mutex g_scratch_mu;
 // device (the first call on that device) and cached; nothing is allocated.
 cudaError_t static_scratch(void** out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    const int dev = current_device();
+    if (dev < 0) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_scratch_mu);
     if (!g_scratch_ptr[dev]) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_static_sort_scratch);
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_sort_scratch);
         if (e != cudaSuccess) return e;
         if (!p) return cudaErrorInvalidSymbol;
         g_scratch_ptr[dev] = p;
@@ -78,4 +81,19 @@ extern "C" gsr_status gsr_sort_bits_static(int num, const int32_t* d_num, int en
     const OrderMap order{kOrderMasked, end_bit, 32};  // tile << 32 | depth bits
     e = launch_sort64(num, d_num, capacity, order, (end_bit + 7) / 8, keys_in, values_in, keys_out, values_out, sc, s);
     return e == cudaSuccess ? GSR_OK : (e == cudaErrorInvalidValue ? GSR_INVALID_ARG : GSR_CUDA_ERROR);
+}
+
+extern "C" gsr_status gsr_sort_bits_static_status(gsr_stream_t stream)
+{
+    // the status word is the first word of the array's header; read it on the
+    // sort's stream, after the sort, into host memory (nothing is allocated)
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t status = 0;
+    cudaError_t e = cudaMemcpyFromSymbolAsync(&status, g_static_sort_scratch, sizeof(status),
+                                              offsetof(WorkspaceHeader, status), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return GSR_CUDA_ERROR;
+    if (status & kErrTimeout) return GSR_TIMEOUT;
+    if (status & kErrBadInput) return GSR_INVALID_ARG;
+    return GSR_OK;
 }

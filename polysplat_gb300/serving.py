@@ -18,8 +18,11 @@ requests (scene, camera, resolution) as they arrive.
   is free.  Every buffer set is allocated once, at start-up, within the
   memory budget; a request is only admitted into a buffer set whose key
   capacity covers its estimated key count.  The estimate is learned per
-  scene from the key counts of finished work.  A request whose keys
-  overflowed is put back with a doubled estimate.
+  scene from the key counts of finished work.  A small-lane batch whose
+  keys overflowed is put back with the true count.  The large lane's buffers
+  hold the largest frame the budget allows: a frame beyond them (or one whose
+  bounded device wait ran out) fails on its own request (``.error``), and the
+  server carries on with the rest of the stream.
 * ``PlainServer`` is the baseline: one ``Rasterizer.forward`` per request in
   arrival order, with a host synchronisation per frame.
 * ``autotune`` picks the tile shape, the batch depth, the lane threshold
@@ -54,10 +57,22 @@ class TuneConfig:
     massive_area: int = 32      # emission dispatch thresholds (tiles of a Gaussian's rectangle)
     huge_area: int = 2048
     variant: int = R.RENDER_PERSISTENT_FUSED
-    # tiles of all views of a small batch: the batch's sort key holds
-    # bits(tiles) tile bits above the depth bits, so a cap at a power of two
-    # can save a whole 8-bit digit pass per batch
+    # key tile ids of all views of a small batch (tiles, or quads with
+    # `quad`): the batch's sort key holds bits(ids) bits above the depth
+    # bits, so a cap at a power of two can save a whole 8-bit digit pass
     max_batch_tiles: int = 1 << 30
+    # small lane: one sort key per 2x2 group of 16x16 tiles (GSR_QUAD_KEYS),
+    # the same image as per-tile keys
+    quad: bool = False
+
+    def key_tiles(self, width: int, height: int) -> int:
+        """Key tile ids of a view in the small lane: its tiles, or its quads."""
+        if self.quad:
+            return ((width + 31) // 32) * ((height + 31) // 32)
+        return ((width + self.block_x - 1) // self.block_x) * ((height + self.block_y - 1) // self.block_y)
+
+    def batch_variant(self) -> int:
+        return self.variant | (R.QUAD_KEYS if self.quad else 0)
 
 
 @dataclasses.dataclass
@@ -72,14 +87,18 @@ class RunStats:
     mean_batch: float = 0.0
     large: int = 0
     retries: int = 0
+    failed: int = 0
 
     def as_dict(self):
         return dataclasses.asdict(self)
 
 
 def _stats(lat_s: Sequence[float], widths: Sequence[int], wall: float, **kw) -> RunStats:
-    lat = np.asarray(lat_s) * 1000.0
-    w = np.asarray(widths)
+    """Throughput and latency percentiles of the completed requests (a
+    failed request has latency None and is left out)."""
+    ok = [i for i, x in enumerate(lat_s) if x is not None]
+    lat = np.asarray([lat_s[i] for i in ok], dtype=np.float64) * 1000.0
+    w = np.asarray([widths[i] for i in ok])
     hd = lat[w == 1920] if len(lat) else lat
     return RunStats(frames_per_s=len(lat) / wall if wall > 0 else 0.0,
                     p50_ms=float(np.percentile(lat, 50)) if len(lat) else math.nan,
@@ -195,7 +214,11 @@ class Server:
     """Continuous-batching server over resident scenes (see module doc)."""
 
     def __init__(self, scenes, device, budget_bytes: int = 60 << 30, config: Optional[TuneConfig] = None,
-                 small_slots: int = 2, large_slots: int = 2, bg=(0.0, 0.0, 0.0)):
+                 small_slots: int = 2, large_slots: int = 2, bg=(0.0, 0.0, 0.0),
+                 large_capacity: Optional[int] = None):
+        """``large_capacity`` caps the key capacity of each large-lane buffer
+        set below what the budget allows (by default the largest power of
+        two up to 2^28 keys whose buffer sets fit in half the budget)."""
         self.scenes = scenes
         self.device = torch.device(device)
         self.cfg = config or TuneConfig()
@@ -208,9 +231,11 @@ class Server:
         large_cap = 1 << 28
         while large_slots * _LargeSlot.device_bytes(large_cap, max_P) > budget_bytes // 2 and large_cap > (1 << 22):
             large_cap //= 2
+        if large_capacity is not None:
+            large_cap = max(1, min(large_cap, int(large_capacity)))
         self.large = [_LargeSlot(large_cap, max_P, self.device) for _ in range(large_slots)]
         left = budget_bytes - large_slots * _LargeSlot.device_bytes(large_cap, max_P)
-        tiles_4k = ((3840 + cfg.block_x - 1) // cfg.block_x) * ((2160 + cfg.block_y - 1) // cfg.block_y)
+        tiles_4k = cfg.key_tiles(3840, 2160)
         max_g = min((1 << 31) - 1, cfg.max_views * max_P)
         small_cap = 1 << 26
         while small_cap > (1 << 20) and small_slots * Batcher.device_bytes(cfg.max_views, small_cap, max_g,
@@ -298,7 +323,7 @@ class Server:
                 r.out = torch.empty((r.cam.height, r.cam.width, 3), dtype=torch.uint8, device=self.device)
                 views.append(View(r.scene, r.cam, self.bg, r.out))
         b = slot["b"]
-        b.render(self.scenes, views, variant=self.cfg.variant, half=True, block_x=self.cfg.block_x,
+        b.render(self.scenes, views, variant=self.cfg.batch_variant(), half=True, block_x=self.cfg.block_x,
                  block_y=self.cfg.block_y, use_graph=True, stream=self.s_small)
         with torch.cuda.stream(self.s_small):
             slot["host"].copy_(slot["ctr"], non_blocking=True)
@@ -315,7 +340,7 @@ class Server:
             if len(out) >= cfg.max_views:
                 break
             e = int(r.est * 1.25)
-            t = ((r.cam.width + cfg.block_x - 1) // cfg.block_x) * ((r.cam.height + cfg.block_y - 1) // cfg.block_y)
+            t = cfg.key_tiles(r.cam.width, r.cam.height)
             P = self.scenes[r.scene].num_vertex
             if out and (keys + e > self.small_cap or g + P > self.max_g or tiles + t > self.tiles_cap
                         or tiles + t > cfg.max_batch_tiles):
@@ -337,13 +362,15 @@ class Server:
         for r in reqs:
             r.cam = Camera.from_spec(r.camera)
             r.out = None
+            r.error = None
+            r.latency_s = None
         n = len(reqs)
         waiting_small: collections.deque = collections.deque()
         waiting_large: collections.deque = collections.deque()
         delivering: collections.deque = collections.deque()  # computed, image copy in flight
         done = 0
         nxt = 0
-        batches, batched, large_n, retries = 0, 0, 0, 0
+        batches, batched, large_n, retries, failed = 0, 0, 0, 0, 0
         t0 = time.perf_counter()
         base = reqs[0].arrival_s if (realtime and reqs) else 0.0
         while done < n:
@@ -363,9 +390,15 @@ class Server:
                     keys, status = int(slot.host[0]), int(slot.host[1])
                     if keys > slot.cap or status:
                         # the large lane's buffers hold the largest frame the
-                        # budget allows: a frame beyond them is an error
-                        raise GsrError(R.GSR_TIMEOUT if status and keys <= slot.cap else R.GSR_OVERFLOW,
-                                       "serving (large lane)", keys)
+                        # budget allows: a frame beyond them fails on its own
+                        # request, and the stream goes on
+                        self.est.observe(r.scene, r.cam, keys)
+                        r.error = GsrError(R.GSR_TIMEOUT if status and keys <= slot.cap else R.GSR_OVERFLOW,
+                                           "serving (large lane)", keys)
+                        r.out = None
+                        self.release(r)
+                        failed += 1
+                        done += 1
                     else:
                         self.est.observe(r.scene, r.cam, keys)
                         delivering.append(r)
@@ -411,7 +444,7 @@ class Server:
                 time.sleep(20e-6)
         wall = time.perf_counter() - t0
         st = _stats([r.latency_s for r in reqs], [r.camera.width for r in reqs], wall, batches=batches,
-                    mean_batch=batched / max(1, batches), large=large_n, retries=retries)
+                    mean_batch=batched / max(1, batches), large=large_n, retries=retries, failed=failed)
         return st
 
     def close(self):
@@ -423,7 +456,12 @@ class Server:
 
 
 # ----------------------------------------------------------------------------- autotuner
-DEFAULT_AXES = [(("block_x", "block_y"), [(32, 16), (32, 32)]),
+# Every candidate renders the reference's 16x16 image (the E2E render's
+# tiles and exit rule): per-tile or quad keys.  Larger tiles change which
+# Gaussians a pixel blends after its tile saturates, and where a Gaussian's
+# conic is indefinite (alpha > 1) that changes the pixel by far more than
+# 2/255, so 32x16 and 32x32 tiles are not candidates.
+DEFAULT_AXES = [("quad", [False, True]),
                 ("large_keys", [2_000_000, 4_000_000, 16_000_000, 1 << 40]),
                 ("max_views", [4, 8, 16]),
                 (("massive_area", "huge_area"), [(64, 4096), (16, 1024)]),

@@ -136,6 +136,46 @@ def test_es_ops_match_depth_first_and_single_pass(cuda_device, case, half):
     assert s["max_abs"] <= 2 and s["psnr"] >= 50.0, s
 
 
+@pytest.mark.parametrize("case,half", [(k, True) for k in CASES] + [("orbit_1280x720", False)])
+def test_es_ops_vs_reference_es_kernels(cuda_device, case, half):
+    """Every buffer of the ES steps against the reference's own ES kernels
+    (preprocessCUDA_ES_PassA / PassB, preprocess.cu:692-1248) and its CUB
+    depth sort, scan and tile sort (sort.cu:151-285), on the same inputs.
+    All integer or copied data: bit-exact.  Within one tile every Gaussian
+    contributes at most one pair, so the tile-sorted values are exact too."""
+    from oracle import refkernels as RK
+
+    if not RK.available():
+        pytest.skip("reference kernels not built")
+    raw, cam = CASES[case][0](), CASES[case][1]()
+    scene = Scene.from_raw(raw, cuda_device)
+    c = Camera.from_spec(cam)
+    cap = 8_000_000
+    m, e = _es_chain(scene, c, half, cap, cuda_device, torch.tensor([0.0, 0.0, 0.0]))
+    r = RK.es_chain(scene, cam, half, cap)
+    assert m == r["m"]
+    u32 = lambda t: t.cpu().numpy().view(np.uint32)
+    # pass A: per-Gaussian counts and records; features of the Gaussians that hit a tile
+    for name in ("tiles_per_gauss", "conic_power_raw", "depth_natural", "rect_bounds"):
+        assert np.array_equal(u32(getattr(e, name)), u32(r[name])), name
+    hit = e.tiles_per_gauss.cpu().numpy() > 0
+    for name in ("xy", "rgbd", "con"):
+        assert np.array_equal(u32(getattr(e, name))[hit], u32(r[name])[hit]), name
+    # depth sort + scan
+    for name in ("identity", "perm", "depth_sorted", "tiles_sorted", "cum", "total"):
+        assert np.array_equal(u32(getattr(e, name)), u32(r[name])), name
+    # pass B: each Gaussian's pairs fill its range [cum[s], cum[s] + count[s])
+    tku, vu = u32(e.tku)[:m], u32(e.vu)[:m]
+    rtku, rvu = u32(r["tku"])[:m], u32(r["vu"])[:m]
+    assert np.array_equal(vu, rvu)  # the range owner's index at every position
+    own = np.repeat(np.arange(scene.num_vertex), e.tiles_sorted.cpu().numpy())
+    assert np.array_equal(tku[np.lexsort((tku, own))], rtku[np.lexsort((rtku, own))])
+    # tile sort and the rebuilt 64-bit keys
+    assert np.array_equal(u32(e.tks)[:m], u32(r["tks"])[:m])
+    assert np.array_equal(u32(e.vs)[:m], u32(r["vs"])[:m])
+    assert np.array_equal(e.ks.cpu().numpy()[:m], r["ks"].cpu().numpy()[:m])
+
+
 def test_es_pass_b_bounded_by_capacity(cuda_device):
     raw, cam = CASES["orbit_1280x720"][0](), CASES["orbit_1280x720"][1]()
     scene = Scene.from_raw(raw, cuda_device)

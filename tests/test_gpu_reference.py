@@ -144,8 +144,9 @@ def test_blend_vs_reference_same_inputs(cuda_device, case, which):
 
 @pytest.mark.parametrize("case", list(CASES))
 def test_whole_frame_vs_reference(cuda_device, case):
-    """Reference pipeline (its preprocess, stable sort, its ranges, its lite
-    render) against this library's fused E2E forward."""
+    """The reference's pipeline end to end (its preprocess, its CUB sort call
+    over bits [0, 32 + msb(tiles)), its ranges and its fused render) against
+    this library's fused E2E forward."""
     from polysplat_gb300 import Rasterizer
 
     scene, spec, ref, _ = _run_both(case, True, cuda_device)
@@ -153,8 +154,13 @@ def test_whole_frame_vs_reference(cuda_device, case):
     W, H = spec.width, spec.height
     tiles = ((W + 15) // 16) * ((H + 15) // 16)
     ks, vs = torch.zeros_like(ref["keys"]), torch.zeros_like(ref["vals"])
-    ws = torch.zeros(ops.get_sort_buffer_size(CAP), dtype=torch.int8, device=cuda_device)
-    ops.sort_gaussian(M, W, H, 16, 16, ws, ref["keys"], ref["vals"], ks, vs)
+    temp = torch.zeros(RK.sort_temp_bytes(M), dtype=torch.int8, device=cuda_device)
+    msb = 16
+    for step in (8, 4, 2, 1):  # getHigherMsb (sort.cu:14-29)
+        msb = msb + step if tiles >> msb else msb - step
+    if tiles >> msb:
+        msb += 1
+    RK.sort(M, 32 + msb, temp, ref["keys"], ref["vals"], ks, vs)
     rr = torch.zeros((tiles, 2), dtype=torch.int32, device=cuda_device)
     RK.tile_ranges(M, ks, tiles, rr)
     out_ref = torch.zeros((H, W, 3), dtype=torch.uint8, device=cuda_device)

@@ -31,21 +31,20 @@ def _mix(n, rate_hz, seed=7):
     return raws, reqs
 
 
-@pytest.mark.parametrize("tile", [(16, 16), (32, 32)])
-def test_served_images_equal_alone(cuda_device, tile):
-    """Both tile shapes the autotuner considers for the batched lane: each
-    request against the single-view forward with the same tile shape."""
-    bx, by = tile
+@pytest.mark.parametrize("quad", [False, True], ids=["tile_keys", "quad_keys"])
+def test_served_images_equal_alone(cuda_device, quad):
+    """Both key layouts the autotuner considers for the batched lane: each
+    request against the single-view 16x16 E2E forward."""
     raws, reqs = _mix(40, 1000.0)
     scs = [Scene.from_raw(r, cuda_device) for r in raws]
-    cfg = TuneConfig(max_views=6, large_keys=400_000, block_x=bx, block_y=by)  # both lanes take work
+    cfg = TuneConfig(max_views=6, large_keys=400_000, quad=quad)  # both lanes take work
     srv = Server(scs, cuda_device, budget_bytes=6 << 30, config=cfg)
     st = srv.run(reqs, realtime=False)
     torch.cuda.synchronize()
     assert st.requests == len(reqs) and st.large > 0 and st.batches > 0 and st.mean_batch > 1.0
     alone = Rasterizer(max(scs, key=lambda s: s.num_vertex), 8_000_000, 1 << 16)
     for r in reqs:
-        img = alone.forward(scs[r.scene], Camera.from_spec(r.camera), torch.zeros(3), block_x=bx, block_y=by,
+        img = alone.forward(scs[r.scene], Camera.from_spec(r.camera), torch.zeros(3),
                             render_variant="preranges_smem_persistent_lite_e2e")
         s = image_stats(r.out.cpu().numpy(), img.cpu().numpy())
         assert s["max_abs"] <= 2 and s["psnr"] >= 50.0, (r.scene, r.camera.width, s)
@@ -72,4 +71,36 @@ def test_autotune_returns_a_serving_config(cuda_device):
     assert len(table) >= 3 and isinstance(best, TuneConfig)
     srv = Server(scs, cuda_device, budget_bytes=6 << 30, config=best)
     assert srv.run(reqs, realtime=False).requests == 16
+    srv.close()
+
+
+def test_large_lane_frame_beyond_its_buffers_fails_alone(cuda_device):
+    """Every request takes the large lane, whose key buffers are capped at
+    the median frame's key count: the bigger frames fail on their own request
+    with the true key count, and every other request is served with its
+    correct image."""
+    raws, reqs = _mix(16, 1000.0, seed=10)
+    scs = [Scene.from_raw(r, cuda_device) for r in raws]
+    alone = Rasterizer(max(scs, key=lambda s: s.num_vertex), 8_000_000, 1 << 16)
+    want = []
+    for r in reqs:
+        img, stt = alone.forward(scs[r.scene], Camera.from_spec(r.camera), torch.zeros(3),
+                                 render_variant="preranges_smem_persistent_lite_e2e", return_stats=True)
+        want.append((img.clone(), int(stt["num_rendered"])))
+    cap = int(np.median([n for _, n in want]))
+    srv = Server(scs, cuda_device, budget_bytes=6 << 30, config=TuneConfig(max_views=4, large_keys=0),
+                 large_capacity=cap)
+    st = srv.run(reqs, realtime=False)
+    torch.cuda.synchronize()
+    n_fail = 0
+    for r, (img, n) in zip(reqs, want):
+        if n > cap:
+            n_fail += 1
+            assert r.error is not None and r.error.status == 1 and r.error.num == n, (n, cap, r.error)
+            assert r.out is None and r.latency_s is None
+        else:
+            assert r.error is None
+            s = image_stats(r.out.cpu().numpy(), img.cpu().numpy())
+            assert s["max_abs"] <= 2 and s["psnr"] >= 50.0, (r.scene, r.camera.width, s)
+    assert 0 < n_fail < len(reqs) and st.failed == n_fail and st.requests == len(reqs) - n_fail
     srv.close()

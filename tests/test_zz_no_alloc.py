@@ -40,14 +40,19 @@ def test_static_sort_matches_workspace_sort(cuda_device, n, end_bit):
     assert L.gsr_sort_bits(n, None, end_bit, _ptr(ws), ws.numel(), _ptr(ku), _ptr(vu), _ptr(ks_ref), _ptr(vs_ref), n,
                            stream) == GSR_OK
     outs = [(torch.full_like(ku, -1), torch.full_like(vu, -1)) for _ in range(2)]
-    free = []
+    free, reserved = [], []
     for ks, vs in outs:  # two calls in a row
         assert L.gsr_sort_bits_static(n, None, end_bit, _ptr(ku), _ptr(vu), _ptr(ks), _ptr(vs), n, stream) == GSR_OK
+        assert L.gsr_sort_bits_static_status(stream) == GSR_OK
         torch.cuda.synchronize()
         free.append(torch.cuda.mem_get_info(cuda_device)[0])
+        reserved.append(torch.cuda.memory_reserved(cuda_device))
     # the scratch array comes with the library's device code (loaded, with
     # lazy module loading, by the first call); a call itself allocates nothing
-    assert free[1] == free[0]
+    assert reserved[1] == reserved[0], "torch's caching allocator grew between the calls"
+    assert free[1] == free[0], (
+        "device free memory changed between two static sorts (%d -> %d bytes) while torch's reserve stayed the "
+        "same: either the entry point allocated, or another context on this GPU did" % (free[0], free[1]))
     for ks, vs in outs:
         assert torch.equal(ks, ks_ref) and torch.equal(vs, vs_ref)
 
@@ -69,6 +74,7 @@ def test_static_sort_device_count(cuda_device):
         ks, vs = torch.full_like(ku, -1), torch.full_like(vu, -1)
         assert L.gsr_sort_bits_static(0, _ptr(d_num), end_bit, _ptr(ku), _ptr(vu), _ptr(ks), _ptr(vs), cap,
                                       stream) == GSR_OK
+        assert L.gsr_sort_bits_static_status(stream) == GSR_OK
         torch.cuda.synchronize()
         assert torch.equal(ks[:n], ks_ref[:n]) and torch.equal(vs[:n], vs_ref[:n])
 
