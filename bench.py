@@ -395,6 +395,50 @@ def forward_line(args, dev, rank, world, dist):
                 "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                 "algorithmic_bytes": abytes, "avg_launch_ms": dur_ms}
 
+    # ---- the same frame with quad keys (one key per 2x2 group of tiles; same image)
+    quad = None
+    if not df:
+        from polysplat_gb300._lib import QUAD_KEYS
+
+        img_tile = out.clone()
+
+        def frame_quad():
+            st = L.gsr_forward(1 | QUAD_KEYS, scene.num_vertex, scene.position.data_ptr(),
+                               scene.shs_half.data_ptr(), 1, scene.opacity.data_ptr(), scene.cov3d.data_ptr(),
+                               cam.width, cam.height, 16, 16, cam_pos, cam_rot, cam.focal_x, cam.focal_y, cam.zFar,
+                               cam.zNear, rast.curr_offset.data_ptr(), ws.data_ptr(), wsb,
+                               rast.gaussian_keys_unsorted.data_ptr(), rast.gaussian_values_unsorted.data_ptr(),
+                               rast.gaussian_keys_sorted.data_ptr(), rast.gaussian_values_sorted.data_ptr(), cap,
+                               rast.points_xy.data_ptr(), rast.rgb_depth.data_ptr(), rast.conic_opacity.data_ptr(),
+                               None, bgc, out.data_ptr(), sh)
+            check(st, "forward (quad keys)")
+
+        for _ in range(max(3, args.warmup)):
+            frame_quad()
+        num_q = ops._read_status(ws, rast.curr_offset, cap, "forward (quad keys)")
+        same = bool(torch.equal(out, img_tile))
+        Kq = max(10, K // 2)
+        check(L.gsr_profile_begin(Kq), "profile_begin")
+        qa, qb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        qa.record(stream)
+        for _ in range(Kq):
+            frame_quad()
+        qb.record(stream)
+        torch.cuda.synchronize()
+        qbuf = (ctypes.c_float * (Kq * MAXS))()
+        nq = L.gsr_profile_read(qbuf, Kq, MAXS)
+        L.gsr_profile_end()
+        q_ms = qa.elapsed_time(qb) / Kq
+        qpasses = nq - 4 if nq > 4 else 0
+        qnames = ["preprocess", "sort_upsweep"] + ["sort_pass%d" % p for p in range(qpasses)] + ["tile_ranges",
+                                                                                                  "render"]
+        q_stages = ({nm: statistics.mean(qbuf[f * MAXS + i] for f in range(Kq)) for i, nm in enumerate(qnames)}
+                    if nq == len(qnames) else None)
+        quad = {"value": world * 1000.0 / max_over_ranks(q_ms, dist, dev), "unit": "frames/s", "ms_per_step": q_ms,
+                "num_keys": num_q, "image_identical_to_tile_keys": same, "stages_ms": q_stages,
+                "what": "the same E2E frame through GSR_QUAD_KEYS: one sort key per 2x2 group of 16x16 tiles"}
+
     # ---- e2e through the public API
     e2e_fps = None
     if not args.quick:
@@ -480,7 +524,8 @@ def forward_line(args, dev, rank, world, dist):
                            "pipeline": args.pipeline,
                            "sort_bits": end_bit, "sort_working_passes": len(working), "l2": "inputs larger than L2 (scene %.0f MB)" %
                            (scene.device_bytes() / 1e6), "parallelism": "replicas" if world > 1 else "single"},
-                "stages_ms": stage_avg, "roofline": roofline, "cpu_baseline": cpu, "reference_gpu": ref_gpu,
+                "stages_ms": stage_avg, "quad_keys": quad, "roofline": roofline, "cpu_baseline": cpu,
+                "reference_gpu": ref_gpu,
                 "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": 60,
                         "d2h_bytes_per_step": cam.width * cam.height * 3 + 4},
                 "gpu_launches": launches_per_frame * K, "clocks": clocks}
@@ -590,7 +635,7 @@ def run_serve(args, dev, rank, world, dist):
     import torch
 
     from polysplat_gb300 import Camera, Rasterizer, Scene, scenes
-    from polysplat_gb300.serving import PlainServer, Server, autotune
+    from polysplat_gb300.serving import PlainServer, Server, TuneConfig, autotune
 
     budget = 60 << 30
     raws, reqs = scenes.serve_mix()
@@ -621,7 +666,9 @@ def run_serve(args, dev, rank, world, dist):
     gc.collect()
     torch.cuda.empty_cache()
 
-    best, table = autotune(scs, reqs[:128], dev, budget_bytes=budget, log=log)
+    start = TuneConfig(quad=True, large_keys=1 << 40, max_views=8, massive_area=64, huge_area=4096,
+                       max_batch_tiles=1 << 14)
+    best, table = autotune(scs, reqs[:128], dev, budget_bytes=budget, log=log, start=start)
     srv = Server(scs, dev, budget, best)
     # warm-up passes over the whole stream: every batch shape's graph is
     # captured and the pinned host pool holds a buffer for every request
@@ -703,8 +750,8 @@ def run_serve(args, dev, rank, world, dist):
             "config": serve_config(raws, reqs, world),
             "gpu_launches": launches, "clocks": clocks, "cpu_baseline": cpu,
             "roofline": dict(fwd["roofline"], workload="plain_3m_1080p (config 1 forward)") if fwd else None,
-            "forward": {k: fwd[k] for k in ("value", "ms_per_step", "stages_ms", "e2e", "reference_gpu", "config")}
-            if fwd else None,
+            "forward": {k: fwd[k] for k in ("value", "ms_per_step", "stages_ms", "quad_keys", "e2e", "reference_gpu",
+                                            "config")} if fwd else None,
             "autotune": {"candidates": len(table), "sample_requests": 128,
                          "best_sample_frames_per_s": max(f for _, f in table)},
             "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 376 * len(reqs),

@@ -52,8 +52,8 @@ typedef enum {
                                          top and bottom 8-row halves stop independently; 16-row tiles only */
 } gsr_render_variant;
 
-/* Flag OR-ed into the variant of gsr_forward and gsr_batcher_render (16x16
- * tiles; not with GSR_RENDER_SPLIT).  No counterpart in the reference: the
+/* Flag OR-ed into the variant of gsr_forward, gsr_forward_depth_first and
+ * gsr_batcher_render (16x16 tiles; not with GSR_RENDER_SPLIT).  No counterpart in the reference: the
  * sort handles one key per 2x2 group of 16x16 tiles ("quad") instead of one
  * per tile.  A key's tile id names the quad (quads numbered row-major,
  * ceil(ceil(W/16)/2) per row); bits 28-31 of its value mark which of the

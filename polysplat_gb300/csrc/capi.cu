@@ -464,14 +464,21 @@ gsr_status gsr_forward_depth_first(int variant, int P, const float* pos, const v
                                    gsr_stream_t stream)
 {
     cudaStream_t s = (cudaStream_t)stream;
+    // GSR_QUAD_KEYS: the pairs name 2x2 groups of 16x16 tiles, same image
+    const bool quad = (variant & GSR_QUAD_KEYS) != 0;
+    variant &= ~GSR_QUAD_KEYS;
     if (!workspace || !curr_offset || !scene_scratch || !valid_tile_shape(block_x, block_y)) return GSR_INVALID_ARG;
     if (variant < 0 || variant > GSR_RENDER_SPLIT) return GSR_INVALID_ARG;
+    if (quad && (block_x != 16 || block_y != 16 || variant == GSR_RENDER_SPLIT || P > (int)kQuadGidMask))
+        return GSR_INVALID_ARG;
     if (workspace_bytes < sort_workspace_bytes(key_capacity) || key_capacity >= (1LL << 30)) return GSR_INVALID_ARG;
     if (P < 0 || scene_scratch_bytes < df_scratch_bytes(P)) return GSR_INVALID_ARG;
     if (key_capacity > 0 && (!tiles_unsorted || !values_unsorted || !tiles_sorted || !values_sorted))
         return GSR_INVALID_ARG;
     if (tiles_unsorted == tiles_sorted || values_unsorted == values_sorted) return GSR_INVALID_ARG;
-    const int tiles = tiles_of(width, height, block_x, block_y);
+    // pair tile ids: tiles, or quads
+    const int tiles = quad ? quad_cols(div_up(width, 16)) * quad_cols(div_up(height, 16))
+                           : tiles_of(width, height, block_x, block_y);
     if (!ranges) {
         if (tiles > kWorkspaceRangeTiles) return GSR_INVALID_ARG;
         ranges = reinterpret_cast<int32_t*>(workspace_ranges(workspace, key_capacity));
@@ -483,6 +490,7 @@ gsr_status gsr_forward_depth_first(int variant, int P, const float* pos, const v
                                       reinterpret_cast<uint64_t*>(tiles_unsorted), values_unsorted, key_capacity,
                                       curr_offset, workspace, workspace_bytes);
     if (st != GSR_OK) return st;
+    p.quad = quad ? 1 : 0;
     profile_frame_begin();
     cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(uint32_t), s);  // status word
     if (e == cudaSuccess) e = cudaMemsetAsync(curr_offset, 0, sizeof(int32_t), s);
@@ -494,7 +502,7 @@ gsr_status gsr_forward_depth_first(int variant, int P, const float* pos, const v
                            reinterpret_cast<int2*>(ranges), s);
     if (e != cudaSuccess) return from_cuda(e);
     st = render_impl(variant, 0, curr_offset, key_capacity, width, height, block_x, block_y, P, points_xy, rgb_depth,
-                     conic_opacity, nullptr, values_sorted, ranges, bg_color, out_color, workspace, s);
+                     conic_opacity, nullptr, values_sorted, ranges, bg_color, out_color, workspace, s, quad);
     if (st == GSR_OK) profile_mark(s);
     return st;
 }

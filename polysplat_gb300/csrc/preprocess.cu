@@ -340,13 +340,13 @@ __device__ __forceinline__ void block_flush(Stage& st, const EmitOut& out, int* 
 // same tests, but each Gaussian's number of hit tiles is counted and written
 // with its depth and test geometry instead of keys.
 //
-// QUAD (emission only): keys name 2x2 groups of tiles, with the hit tiles as a
-// mask in the value (PreprocessParams::quad); the tile rectangle, the dispatch
-// and every tile test are the per-tile emission's.
+// QUAD: keys name 2x2 groups of tiles, with the hit tiles as a mask in the
+// value (PreprocessParams::quad), and the counting pass counts those quads;
+// the tile rectangle, the dispatch and every tile test are the per-tile
+// emission's.
 template <bool HALF, bool COUNT, bool VIEWS, bool QUAD = false>
 __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __grid_constant__ PreprocessParams a0)
 {
-    static_assert(!(QUAD && COUNT), "quad keys are an emission mode");
     // VIEWS: the views' blocks follow one another along the grid (parameter
     // blocks in device memory); a block past the last view has no work
     int vi = 0, lblock = (int)blockIdx.x;
@@ -518,8 +518,13 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
                                            ? quad_mask(qx, qy, make_int2(x_lo, y_lo), make_int2(x_hi, y_hi), a.bx,
                                                        a.by, c, q, pw)
                                            : 0u;
-                    const uint64_t key = ((uint64_t)(uint32_t)(a.tile_base + qy * qgx + qx) << 32) | db;
-                    stage_emit(st, out, m != 0u, key, gid | (m << kQuadShift), lane);
+                    if (COUNT) {
+                        const unsigned mm = __ballot_sync(GSR_FULL_MASK, m != 0u);
+                        if (lane == 0) s_cnt[warp][i] += __popc(mm);
+                    } else {
+                        const uint64_t key = ((uint64_t)(uint32_t)(a.tile_base + qy * qgx + qx) << 32) | db;
+                        stage_emit(st, out, m != 0u, key, gid | (m << kQuadShift), lane);
+                    }
                 }
             }
         } else {
@@ -632,12 +637,31 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
     }
 
     if (COUNT) {
+        // The reference's ES layout writes a Gaussian's depth (and records)
+        // only where its pass A marks the Gaussian valid, which depends on
+        // that pass's warp-level dispatch (preprocess.cu:800-874, 957-985):
+        // always for a one-tile rectangle; for larger ones always on its
+        // pooled path, but on its per-Gaussian path (taken when the warp
+        // holds at most two multi-tile Gaussians or one of at least 32
+        // tiles) only when a tile was hit.  The others get depth FLT_MAX.
+        // Both passes give a warp the same 32 consecutive Gaussians, and the
+        // ES layout runs without the large-Gaussian queue, so s_cnt holds the
+        // final counts here.
+        bool ref_valid = false;
+        if (a.df.ref_layout) {  // uniform over the warp
+            const bool multi_g = was_valid && area > 1;
+            const unsigned mg = __ballot_sync(GSR_FULL_MASK, multi_g);
+            const int max_area = __reduce_max_sync(GSR_FULL_MASK, multi_g ? area : 0);
+            const bool per_gaussian_path = __popc(mg) <= 2 || max_area >= 32;
+            ref_valid = (was_valid && area == 1) || (multi_g && (!per_gaussian_path || s_cnt[warp][lane] > 0u));
+        }
         // (4') records of the counting pass (queued Gaussians get their count
         // from the massive kernel, which runs next)
         if (idx < a.P) {
             a.df.count[idx] = was_valid ? s_cnt[warp][lane] : 0u;
+            if (a.df.ref_layout && !ref_valid) a.df.dkey[idx] = 0x7F7FFFFFu;  // FLT_MAX (preprocess.cu:983)
+            if (was_valid && (!a.df.ref_layout || ref_valid)) a.df.dkey[idx] = depth_bits;
             if (was_valid) {
-                a.df.dkey[idx] = depth_bits;
                 a.df.geo[idx] = make_float4(conic.x, conic.y, conic.z, power);
                 if (a.df.ref_layout)  // (rect_min, rect_max) packed as (x | y << 16), preprocess.cu:975-977
                     a.df.rect[idx] = make_int2((int)((uint32_t)rect_min.x | ((uint32_t)rect_min.y << 16)),
@@ -646,8 +670,6 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
                     a.df.rect[idx] = make_int2((int)((uint32_t)rect_min.x | ((uint32_t)rect_max.x << 16)),
                                                (int)((uint32_t)rect_min.y | ((uint32_t)rect_max.y << 16) |
                                                      (queued ? 0x80000000u : 0u)));
-            } else if (a.df.ref_layout) {
-                a.df.dkey[idx] = 0x7F7FFFFFu;  // FLT_MAX: culled Gaussians sort last (preprocess.cu:983)
             }
         }
     } else {
@@ -1008,10 +1030,13 @@ enum : int { kMassiveEmit64 = 0, kMassiveCount = 1, kMassiveEmitDf = 2 };
 // time with all 256 threads, then each warp takes large rectangles on its
 // own.  MODE: emit 64-bit keys, count the hit tiles (depth-first counting
 // pass), or write depth-first pairs at the Gaussian's offset.
+//
+// QUAD: the sweeps run over quads (sweep_cta_quad / sweep_warp_quad); a quad
+// whose mask is not empty counts as one, and is written as (quad id, index |
+// mask << kQuadShift).
 template <int MODE, bool VIEWS, bool QUAD = false>
 __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant__ PreprocessParams a, const DfEmit df)
 {
-    static_assert(!QUAD || MODE == kMassiveEmit64, "quad keys are an emission mode");
     __shared__ uint64_t s_keys[MODE == kMassiveEmit64 ? kWarps : 1][kStage];
     __shared__ uint32_t s_vals[MODE == kMassiveEmit64 ? kWarps : 1][kStage];
     __shared__ int s_fill[kWarps];
@@ -1056,9 +1081,14 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
             });
         } else if (MODE == kMassiveCount) {
             uint32_t cnt = 0;
-            sweep_cta(me, a, s_band, lane, warp, [&](bool v, int, int) {
-                cnt += __popc(__ballot_sync(GSR_FULL_MASK, v));
-            });
+            if (QUAD)
+                sweep_cta_quad(me, a, s_band, lane, warp, [&](bool v, int, int, uint32_t) {
+                    cnt += __popc(__ballot_sync(GSR_FULL_MASK, v));
+                });
+            else
+                sweep_cta(me, a, s_band, lane, warp, [&](bool v, int, int) {
+                    cnt += __popc(__ballot_sync(GSR_FULL_MASK, v));
+                });
             if (lane == 0) s_wcnt[warp] = cnt;
             __syncthreads();
             if (threadIdx.x == 0) {
@@ -1071,7 +1101,8 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
             const uint32_t count = a.df.count[gid];
             if (count == 0u) continue;
             const long long base = df.offsets[df.rank[gid]];
-            sweep_cta(me, a, s_band, lane, warp, [&](bool v, int x, int y) {
+            // a pair (tile id, value) at the next of the Gaussian's own slots
+            auto put = [&](bool v, uint32_t tile, uint32_t val) {
                 const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
                 if (!m) return;
                 uint32_t w0 = 0;
@@ -1079,10 +1110,19 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
                 w0 = __shfl_sync(GSR_FULL_MASK, w0, 0);
                 const uint32_t k = w0 + __popc(m & lanemask_lt());
                 if (v && k < count && base + k < df.cap) {  // never past the Gaussian's own slots
-                    df.tiles[base + k] = (uint32_t)(y * a.gx + x);
-                    df.vals[base + k] = gid;
+                    df.tiles[base + k] = tile;
+                    df.vals[base + k] = val;
                 }
-            });
+            };
+            if (QUAD) {
+                const int qgx = quad_cols(a.gx);
+                sweep_cta_quad(me, a, s_band, lane, warp, [&](bool v, int qx, int qy, uint32_t m) {
+                    put(v, (uint32_t)(qy * qgx + qx), gid | (m << kQuadShift));
+                });
+            } else {
+                sweep_cta(me, a, s_band, lane, warp,
+                          [&](bool v, int x, int y) { put(v, (uint32_t)(y * a.gx + x), gid); });
+            }
             // sweep_cta ended on a barrier, so s_pos is final; every thread
             // reads it before thread 0 resets it for the next entry
             const uint32_t filled = s_pos;
@@ -1119,22 +1159,34 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
             });
         } else if (MODE == kMassiveCount) {
             uint32_t cnt = 0;
-            sweep_warp(me, a, lane, [&](bool v, int, int) { cnt += __popc(__ballot_sync(GSR_FULL_MASK, v)); });
+            if (QUAD)
+                sweep_warp_quad(me, a, lane,
+                                [&](bool v, int, int, uint32_t) { cnt += __popc(__ballot_sync(GSR_FULL_MASK, v)); });
+            else
+                sweep_warp(me, a, lane, [&](bool v, int, int) { cnt += __popc(__ballot_sync(GSR_FULL_MASK, v)); });
             if (lane == 0) a.df.count[gid] = cnt;
         } else {
             const uint32_t count = a.df.count[gid];
             if (count == 0u) continue;
             const long long base = df.offsets[df.rank[gid]];
             uint32_t wpos = 0;
-            sweep_warp(me, a, lane, [&](bool v, int x, int y) {
+            auto put = [&](bool v, uint32_t tile, uint32_t val) {
                 const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
                 const uint32_t k = wpos + __popc(m & lanemask_lt());
                 if (v && k < count && base + k < df.cap) {
-                    df.tiles[base + k] = (uint32_t)(y * a.gx + x);
-                    df.vals[base + k] = gid;
+                    df.tiles[base + k] = tile;
+                    df.vals[base + k] = val;
                 }
                 wpos += __popc(m);
-            });
+            };
+            if (QUAD) {
+                const int qgx = quad_cols(a.gx);
+                sweep_warp_quad(me, a, lane, [&](bool v, int qx, int qy, uint32_t m) {
+                    put(v, (uint32_t)(qy * qgx + qx), gid | (m << kQuadShift));
+                });
+            } else {
+                sweep_warp(me, a, lane, [&](bool v, int x, int y) { put(v, (uint32_t)(y * a.gx + x), gid); });
+            }
             for (uint32_t k = wpos + lane; k < count; k += 32)
                 if (base + k < df.cap) {
                     df.tiles[base + k] = kTileSentinel;
@@ -1145,40 +1197,132 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
     if (MODE == kMassiveEmit64) block_flush(st, out, s_fill, s_base, lane, warp);
 }
 
-// Depth-first emission of the Gaussians that were not queued: one thread per
-// Gaussian, taken in depth order, writes its (tile, index) pairs from its
-// offset on.  Same tile test as the counting pass, so exactly count[g] pairs.
-__global__ __launch_bounds__(256) void k_df_emit_small(const PreprocessParams a, const DfEmit df,
+// Depth-first emission of the Gaussians that were not queued, taken in depth
+// order: each writes its (tile, index) pairs from its offset on.  Each warp
+// takes 32 consecutive Gaussians of the order; a rectangle under
+// massive_area tiles is swept by its own thread, a larger one (a Gaussian
+// the full large-Gaussian queue turned away) by the whole warp in 8 x 4
+// windows, as the counting pass swept it.  Same tile test as the counting
+// pass, so exactly count[g] pairs; slots a Gaussian cannot fill are padded.
+//
+// QUAD: the Gaussian's quads, each with a non-empty mask, as (quad id, index |
+// mask << kQuadShift).
+template <bool QUAD>
+__global__ __launch_bounds__(256, 2) void k_df_emit_small(const PreprocessParams a, const DfEmit df,
                                                        const uint32_t* __restrict__ d_v,
                                                        const uint32_t* __restrict__ sgids)
 {
     const int V = (int)min(*d_v, (uint32_t)a.P);
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < V; s += gridDim.x * blockDim.x) {
-        const uint32_t gid = __ldg(sgids + s);
-        if (gid >= (uint32_t)a.P) continue;
-        const int2 r = __ldg(a.df.rect + gid);
-        if ((uint32_t)r.y & 0x80000000u) continue;  // queued: the massive kernel writes it
-        const int x0 = r.x & 0xFFFF, x1 = (int)((uint32_t)r.x >> 16);
-        const int y0 = r.y & 0xFFFF, y1 = (int)(((uint32_t)r.y >> 16) & 0x7FFFu);
-        const float4 g = __ldg(a.df.geo + gid);
-        const float2 ctr = __ldg(a.points_xy + gid);
-        const float3 con = {g.x, g.y, g.z};
-        long long pos = __ldg(df.offsets + s);
-        const long long lim = pos + __ldg(a.df.count + gid);  // the Gaussian's own slots
-        for (int y = y0; y < y1; y++)
-            for (int x = x0; x < x1; x++) {
-                if (!tile_hit(x, y, a.bx, a.by, ctr, con, g.w)) continue;
-                if (pos < lim && pos < df.cap) {
-                    df.tiles[pos] = (uint32_t)(y * a.gx + x);
-                    df.vals[pos] = gid;
+    const unsigned lane = threadIdx.x & 31u;
+    const int qgx = quad_cols(a.gx);
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long s0 = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; s0 < V;
+         s0 += warps * 32) {
+        const long long s = s0 + lane;
+        uint32_t gid = 0u, count = 0u;
+        int x0 = 0, x1 = 0, y0 = 0, y1 = 0;
+        long long pos = 0;
+        bool own = false, wide = false;
+        if (s < V) {
+            gid = __ldg(sgids + s);
+            if (gid < (uint32_t)a.P) {
+                const int2 r = __ldg(a.df.rect + gid);
+                if (!((uint32_t)r.y & 0x80000000u)) {  // queued ones: the massive kernel writes them
+                    x0 = r.x & 0xFFFF;
+                    x1 = (int)((uint32_t)r.x >> 16);
+                    y0 = r.y & 0xFFFF;
+                    y1 = (int)(((uint32_t)r.y >> 16) & 0x7FFFu);
+                    pos = __ldg(df.offsets + s);
+                    count = __ldg(a.df.count + gid);
+                    wide = (x1 - x0) * (y1 - y0) >= a.massive_area;
+                    own = !wide;
                 }
-                pos++;
             }
-        for (; pos < lim; pos++)  // pad unfilled slots
-            if (pos < df.cap) {
-                df.tiles[pos] = kTileSentinel;
-                df.vals[pos] = kTileSentinel;
+        }
+        const float4 g = own || wide ? __ldg(a.df.geo + gid) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float2 ctr = own || wide ? __ldg(a.points_xy + gid) : make_float2(0.f, 0.f);
+        if (own) {
+            const float3 con = {g.x, g.y, g.z};
+            const long long lim = pos + count;  // the Gaussian's own slots
+            if (QUAD) {
+                for (int qy = quad_lo(y0); qy < quad_hi(y1); qy++)
+                    for (int qx = quad_lo(x0); qx < quad_hi(x1); qx++) {
+                        const uint32_t m =
+                            quad_mask(qx, qy, make_int2(x0, y0), make_int2(x1, y1), a.bx, a.by, ctr, con, g.w);
+                        if (!m) continue;
+                        if (pos < lim && pos < df.cap) {
+                            df.tiles[pos] = (uint32_t)(qy * qgx + qx);
+                            df.vals[pos] = gid | (m << kQuadShift);
+                        }
+                        pos++;
+                    }
+            } else {
+                for (int y = y0; y < y1; y++)
+                    for (int x = x0; x < x1; x++) {
+                        if (!tile_hit(x, y, a.bx, a.by, ctr, con, g.w)) continue;
+                        if (pos < lim && pos < df.cap) {
+                            df.tiles[pos] = (uint32_t)(y * a.gx + x);
+                            df.vals[pos] = gid;
+                        }
+                        pos++;
+                    }
             }
+            for (; pos < lim; pos++)  // pad unfilled slots
+                if (pos < df.cap) {
+                    df.tiles[pos] = kTileSentinel;
+                    df.vals[pos] = kTileSentinel;
+                }
+        }
+        // the wide rectangles, one after another, by the whole warp
+        unsigned todo = __ballot_sync(GSR_FULL_MASK, wide);
+        while (todo) {
+            const int i = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const uint32_t wg = __shfl_sync(GSR_FULL_MASK, gid, i);
+            const uint32_t wcount = __shfl_sync(GSR_FULL_MASK, count, i);
+            const long long base = __shfl_sync(GSR_FULL_MASK, pos, i);
+            const int2 rmin = make_int2(__shfl_sync(GSR_FULL_MASK, x0, i), __shfl_sync(GSR_FULL_MASK, y0, i));
+            const int2 rmax = make_int2(__shfl_sync(GSR_FULL_MASK, x1, i), __shfl_sync(GSR_FULL_MASK, y1, i));
+            const float2 c = {__shfl_sync(GSR_FULL_MASK, ctr.x, i), __shfl_sync(GSR_FULL_MASK, ctr.y, i)};
+            const float3 q = {__shfl_sync(GSR_FULL_MASK, g.x, i), __shfl_sync(GSR_FULL_MASK, g.y, i),
+                              __shfl_sync(GSR_FULL_MASK, g.z, i)};
+            const float pw = __shfl_sync(GSR_FULL_MASK, g.w, i);
+            uint32_t wpos = 0;
+            auto put = [&](bool v, uint32_t tile, uint32_t val) {
+                const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
+                const uint32_t k = wpos + __popc(m & lanemask_lt());
+                if (v && k < wcount && base + k < df.cap) {
+                    df.tiles[base + k] = tile;
+                    df.vals[base + k] = val;
+                }
+                wpos += __popc(m);
+            };
+            const int tx = (int)(lane & 7u), ty = (int)(lane >> 3);
+            if (QUAD) {
+                const int qx_lo = quad_lo(rmin.x), qx_hi = quad_hi(rmax.x);
+                const int qy_lo = quad_lo(rmin.y), qy_hi = quad_hi(rmax.y);
+                for (int yy = qy_lo; yy < qy_hi; yy += 4)
+                    for (int xx = qx_lo; xx < qx_hi; xx += 8) {
+                        const int qx = xx + tx, qy = yy + ty;
+                        const uint32_t m = (qx < qx_hi && qy < qy_hi)
+                                               ? quad_mask(qx, qy, rmin, rmax, a.bx, a.by, c, q, pw)
+                                               : 0u;
+                        put(m != 0u, (uint32_t)(qy * qgx + qx), wg | (m << kQuadShift));
+                    }
+            } else {
+                for (int yy = rmin.y; yy < rmax.y; yy += 4)
+                    for (int xx = rmin.x; xx < rmax.x; xx += 8) {
+                        const int x = xx + tx, y = yy + ty;
+                        const bool v = x < rmax.x && y < rmax.y && tile_hit(x, y, a.bx, a.by, c, q, pw);
+                        put(v, (uint32_t)(y * a.gx + x), wg);
+                    }
+            }
+            for (uint32_t k = wpos + lane; k < wcount; k += 32)  // pad unfilled slots
+                if (base + k < df.cap) {
+                    df.tiles[base + k] = kTileSentinel;
+                    df.vals[base + k] = kTileSentinel;
+                }
+        }
     }
 }
 
@@ -1288,9 +1432,12 @@ static cudaError_t preprocess_common(const PreprocessParams& p, bool half_sh, bo
         cudaError_t e = cudaMemsetAsync(p.mq.count, 0, kPreprocessRegionBytes, stream);
         if (e != cudaSuccess) return e;
     }
-    if (p.quad && (count || p.bx != 16 || p.by != 16)) return cudaErrorInvalidValue;
+    if (p.quad && (p.bx != 16 || p.by != 16 || p.df.ref_layout)) return cudaErrorInvalidValue;
     const int grid = div_up(p.P, kThreads);
-    if (count) {
+    if (count && p.quad) {
+        if (half_sh) k_preprocess<true, true, false, true><<<grid, kThreads, 0, stream>>>(p);
+        else k_preprocess<false, true, false, true><<<grid, kThreads, 0, stream>>>(p);
+    } else if (count) {
         if (half_sh) k_preprocess<true, true, false><<<grid, kThreads, 0, stream>>>(p);
         else k_preprocess<false, true, false><<<grid, kThreads, 0, stream>>>(p);
     } else if (p.quad) {
@@ -1303,7 +1450,10 @@ static cudaError_t preprocess_common(const PreprocessParams& p, bool half_sh, bo
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.mq.capacity <= 0) return e;
     const DfEmit none{nullptr, nullptr, nullptr, nullptr, 0};
-    if (count) k_emit_massive<kMassiveCount, false><<<emit_grid(k_emit_massive<kMassiveCount, false>), kThreads, 0, stream>>>(p, none);
+    if (count && p.quad)
+        k_emit_massive<kMassiveCount, false, true>
+            <<<emit_grid(k_emit_massive<kMassiveCount, false, true>), kThreads, 0, stream>>>(p, none);
+    else if (count) k_emit_massive<kMassiveCount, false><<<emit_grid(k_emit_massive<kMassiveCount, false>), kThreads, 0, stream>>>(p, none);
     else if (p.quad)
         k_emit_massive<kMassiveEmit64, false, true>
             <<<emit_grid(k_emit_massive<kMassiveEmit64, false, true>), kThreads, 0, stream>>>(p, none);
@@ -1354,7 +1504,12 @@ cudaError_t launch_df_emit_massive(const PreprocessParams& p, const uint32_t* of
     // takes the queue again through the second pair of heads (cleared with
     // the rest of the preprocess region before the counting pass)
     const DfEmit df{offsets, rank, tiles, vals, cap};
-    k_emit_massive<kMassiveEmitDf, false><<<emit_grid(k_emit_massive<kMassiveEmitDf, false>), kThreads, 0, stream>>>(p, df);
+    if (p.quad)
+        k_emit_massive<kMassiveEmitDf, false, true>
+            <<<emit_grid(k_emit_massive<kMassiveEmitDf, false, true>), kThreads, 0, stream>>>(p, df);
+    else
+        k_emit_massive<kMassiveEmitDf, false>
+            <<<emit_grid(k_emit_massive<kMassiveEmitDf, false>), kThreads, 0, stream>>>(p, df);
     return cudaGetLastError();
 }
 
@@ -1428,7 +1583,8 @@ cudaError_t launch_df_emit_small(const PreprocessParams& p, const uint32_t* d_v,
     if (p.P <= 0) return cudaSuccess;
     const DfEmit df{offsets, nullptr, tiles, vals, cap};
     const int grid = std::min(div_up(p.P, 256), device_sm_count() * 8);
-    k_df_emit_small<<<grid, 256, 0, stream>>>(p, df, d_v, sgids);
+    if (p.quad) k_df_emit_small<true><<<grid, 256, 0, stream>>>(p, df, d_v, sgids);
+    else k_df_emit_small<false><<<grid, 256, 0, stream>>>(p, df, d_v, sgids);
     return cudaGetLastError();
 }
 

@@ -108,40 +108,70 @@ __device__ __forceinline__ int warp_bound(const uint64_t* __restrict__ keys, int
     return lo + __popc(__ballot_sync(GSR_FULL_MASK, pred));
 }
 
-// Stage Gaussians vals[pos, pos+cnt) into ring half `b`; returns how many
-// were staged.  QUAD: only the values with bit `sub_bit` set (the Gaussians
-// of this warp's tile of the quad) are staged, packed to the front.
+// Stage the next Gaussians of the tile's list, from position `pos` on, into
+// ring half `b`, and advance `pos` past them; returns how many were staged.
+// Per-tile lists: the next min(32, end - pos).  QUAD: the quad's list is
+// scanned from `pos` on until 32 values with bit `sub_bit` set (the
+// Gaussians of this warp's tile of the quad) are staged, in list order, or
+// the list ends -- so a batch is as full as in a per-tile list.
 template <bool TMA, bool QUAD = false>
-__device__ __forceinline__ int stage_batch(WarpRing& R, int b, const RenderParams& p, int pos, int cnt,
+__device__ __forceinline__ int stage_batch(WarpRing& R, int b, const RenderParams& p, int& pos, int end,
                                            unsigned lane, bool& bad, uint32_t sub_bit = 0u)
 {
     __syncwarp();
     if (TMA) fence_proxy_async_smem();
+    if (QUAD) {
+        static_assert(!QUAD || !TMA, "quad renders stage with cp.async");
+        int filled = 0;
+        while (filled < kBatch && pos < end) {
+            const int cnt = min(kBatch, end - pos);
+            uint32_t v = 0u;
+            if ((int)lane < cnt) v = __ldg(p.vals + pos + lane);
+            const bool hit = (int)lane < cnt && (v & sub_bit) != 0u;
+            const unsigned hits = __ballot_sync(GSR_FULL_MASK, hit);
+            const int room = kBatch - filled;
+            const int rank = __popc(hits & lanemask_lt());
+            uint32_t gid = v & kQuadGidMask;
+            if (hit && rank < room) {
+                if (gid < (uint32_t)p.P) {
+                    const int slot = filled + rank;
+                    cp_async_16(&R.con[b][slot], p.con + gid);
+                    cp_async_16(&R.rgbd[b][slot], p.rgbd + gid);
+                    cp_async_8(&R.xy2[b][slot], p.xy + gid);
+                    R.sel[b][slot] = 0u;
+                } else {  // index outside the feature arrays: a transparent stand-in
+                    bad = true;
+                    const int slot = filled + rank;
+                    R.con[b][slot] = make_float4(0.f, 0.f, 0.f, -1e30f);
+                    R.rgbd[b][slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    R.xy2[b][slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    R.sel[b][slot] = 0u;
+                }
+            }
+            const int n = __popc(hits);
+            if (n <= room) {
+                pos += cnt;
+                filled += n;
+            } else {
+                // the batch is full: resume right after its last Gaussian
+                pos += __ffs(__ballot_sync(GSR_FULL_MASK, hit && rank == room - 1));
+                filled = kBatch;
+            }
+        }
+        cp_async_commit();
+        return filled;
+    }
+    const int cnt = min(kBatch, end - pos);
+    pos += cnt;
+    const int base = pos - cnt;
     uint32_t gid = 0;
     bool ok = (int)lane < cnt;
     if (ok) {
-        gid = __ldg(p.vals + pos + lane);
-        if (QUAD) {
-            ok = (gid & sub_bit) != 0u;
-            gid &= kQuadGidMask;
-        }
-        if (ok && gid >= (uint32_t)p.P) {  // index outside the feature arrays: skip it
+        gid = __ldg(p.vals + base + lane);
+        if (gid >= (uint32_t)p.P) {  // index outside the feature arrays: skip it
             ok = false;
             bad = true;
         }
-    }
-    if (QUAD) {
-        static_assert(!QUAD || !TMA, "quad renders stage with cp.async");
-        const unsigned keep = __ballot_sync(GSR_FULL_MASK, ok);
-        if (ok) {
-            const int slot = __popc(keep & lanemask_lt());
-            cp_async_16(&R.con[b][slot], p.con + gid);
-            cp_async_16(&R.rgbd[b][slot], p.rgbd + gid);
-            cp_async_8(&R.xy2[b][slot], p.xy + gid);
-            R.sel[b][slot] = 0u;
-        }
-        cp_async_commit();
-        return __popc(keep);
     }
     const bool pair_ok = ok && (gid | 1u) < (uint32_t)p.P;
     if (TMA) {
@@ -343,19 +373,20 @@ __global__ __launch_bounds__(kRenderWarps * 32) void k_render(const RenderParams
         bool blended_any = false;  // QUAD: the tile's own list is not empty
         if (total > 0) {
             int cur = 0;
-            int staged = stage_batch<TMA, QUAD>(R, 0, p, start, min(kBatch, total), lane, bad, sub_bit);
+            int scan = start;  // next list position to stage from
+            int staged = stage_batch<TMA, QUAD>(R, 0, p, scan, end, lane, bad, sub_bit);
             int processed = 0;
             bool half_done = false;  // EXIT 1: this lane's half has stopped
-            for (int pos = start; pos < end; pos += kBatch) {
+            while (staged > 0) {
                 const int bsize = staged;
-                const int npos = pos + kBatch;
-                const int nsize = max(0, min(kBatch, end - npos));
                 if (!wait_batch<TMA>(R, cur, phase_bits)) {
                     timed_out = true;
                     break;
                 }
-                if (nsize > 0) staged = stage_batch<TMA, QUAD>(R, cur ^ 1, p, npos, nsize, lane, bad, sub_bit);
-                blended_any = blended_any || bsize > 0;
+                const int nsize = scan < end ? stage_batch<TMA, QUAD>(R, cur ^ 1, p, scan, end, lane, bad, sub_bit)
+                                             : 0;
+                staged = nsize;
+                blended_any = true;
                 bool exit_now = false;
                 for (int g = 0; g < bsize; g++) {
                     const float4 co = R.con[cur][g];

@@ -361,6 +361,8 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortJob<K> a, int pass
             uint32_t spins = 0;
             bool done = j < 0;
             while (!done) {
+                // four predecessors per round trip: measured faster than 8
+                // (+6%) or 16 (+25%) at 9.2 M keys
                 uint32_t v[4];
 #pragma unroll
                 for (int k = 0; k < 4; k++)

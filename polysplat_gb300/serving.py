@@ -61,7 +61,7 @@ class TuneConfig:
     # `quad`): the batch's sort key holds bits(ids) bits above the depth
     # bits, so a cap at a power of two can save a whole 8-bit digit pass
     max_batch_tiles: int = 1 << 30
-    # small lane: one sort key per 2x2 group of 16x16 tiles (GSR_QUAD_KEYS),
+    # both lanes: one sort key per 2x2 group of 16x16 tiles (GSR_QUAD_KEYS),
     # the same image as per-tile keys
     quad: bool = False
 
@@ -72,6 +72,7 @@ class TuneConfig:
         return ((width + self.block_x - 1) // self.block_x) * ((height + self.block_y - 1) // self.block_y)
 
     def batch_variant(self) -> int:
+        """The render variant of both lanes, with GSR_QUAD_KEYS when `quad`."""
         return self.variant | (R.QUAD_KEYS if self.quad else 0)
 
 
@@ -127,9 +128,10 @@ class KeyEstimator:
     """Keys per pixel of each scene, learned from finished frames (the
     largest rate seen, so an estimate errs high)."""
 
-    def __init__(self, scenes):
-        # start from about 2.5 keys per pixel per million Gaussians
-        self.rate = [2.5e-6 * max(1, s.num_vertex) for s in scenes]
+    def __init__(self, scenes, per_million: float = 2.5):
+        # start from `per_million` keys per pixel per million Gaussians
+        # (about 2.5 per-tile keys; a quad key stands for about 2.5 of them)
+        self.rate = [per_million * 1e-6 * max(1, s.num_vertex) for s in scenes]
 
     def __call__(self, scene: int, cam) -> int:
         return int(self.rate[scene] * _pixels(cam)) + 4096
@@ -223,7 +225,7 @@ class Server:
         self.device = torch.device(device)
         self.cfg = config or TuneConfig()
         self.bg = [float(x) for x in bg]
-        self.est = KeyEstimator(scenes)
+        self.est = KeyEstimator(scenes, 1.0 if self.cfg.quad else 2.5)
         cfg = self.cfg
         max_P = max(s.num_vertex for s in scenes)
         # buffer sets, sized within the budget: large lane first (one 4K frame
@@ -282,7 +284,7 @@ class Server:
         cr = (ctypes.c_float * 9)(*cam.rotation.reshape(-1).tolist())
         bgc = (ctypes.c_float * 3)(*self.bg)
         st = L.gsr_forward_depth_first(
-            self.cfg.variant, s.num_vertex, s.position.data_ptr(), s.shs_half.data_ptr(), 1, s.opacity.data_ptr(),
+            self.cfg.batch_variant(), s.num_vertex, s.position.data_ptr(), s.shs_half.data_ptr(), 1, s.opacity.data_ptr(),
             s.cov3d.data_ptr(), cam.width, cam.height, self.cfg.block_x, self.cfg.block_y, cp, cr, cam.focal_x,
             cam.focal_y, cam.zFar, cam.zNear, slot.counter.data_ptr(), slot.ws.data_ptr(), slot.ws.numel(),
             slot.scratch.data_ptr(), slot.scratch.numel(), slot.tiles_u.data_ptr(), slot.vals_u.data_ptr(),
@@ -462,10 +464,10 @@ class Server:
 # conic is indefinite (alpha > 1) that changes the pixel by far more than
 # 2/255, so 32x16 and 32x32 tiles are not candidates.
 DEFAULT_AXES = [("quad", [False, True]),
-                ("large_keys", [2_000_000, 4_000_000, 16_000_000, 1 << 40]),
+                ("large_keys", [4_000_000, 16_000_000, 1 << 40]),
                 ("max_views", [4, 8, 16]),
                 (("massive_area", "huge_area"), [(64, 4096), (16, 1024)]),
-                ("max_batch_tiles", [1 << 13, 1 << 14])]
+                ("max_batch_tiles", [1 << 13, 1 << 14, 1 << 15])]
 
 
 def autotune(scenes, sample_reqs, device, budget_bytes: int = 60 << 30, log=None, axes=None,

@@ -155,12 +155,15 @@ def test_es_ops_vs_reference_es_kernels(cuda_device, case, half):
     r = RK.es_chain(scene, cam, half, cap)
     assert m == r["m"]
     u32 = lambda t: t.cpu().numpy().view(np.uint32)
-    # pass A: per-Gaussian counts and records; features of the Gaussians that hit a tile
-    for name in ("tiles_per_gauss", "conic_power_raw", "depth_natural", "rect_bounds"):
+    # pass A: counts and depths of every Gaussian; the records pass B reads
+    # (conic + power, rectangle) and the features, for the Gaussians that
+    # hit a tile (the reference leaves the other rows as they were)
+    for name in ("tiles_per_gauss", "depth_natural"):
         assert np.array_equal(u32(getattr(e, name)), u32(r[name])), name
     hit = e.tiles_per_gauss.cpu().numpy() > 0
-    for name in ("xy", "rgbd", "con"):
-        assert np.array_equal(u32(getattr(e, name))[hit], u32(r[name])[hit]), name
+    for name in ("conic_power_raw", "rect_bounds", "xy", "rgbd", "con"):
+        mine, ref = u32(getattr(e, name))[hit], u32(r[name])[hit]
+        assert np.array_equal(mine, ref), (name, int((mine != ref).any(axis=-1).sum()))
     # depth sort + scan
     for name in ("identity", "perm", "depth_sorted", "tiles_sorted", "cum", "total"):
         assert np.array_equal(u32(getattr(e, name)), u32(r[name])), name

@@ -124,6 +124,59 @@ def test_quad_keys_expand_to_per_tile_keys_and_same_image(cuda_device, name, raw
     assert np.all(sq[1:] >= sq[:-1])
 
 
+def _depth_first(fr, cam, variant, scratch):
+    """gsr_forward_depth_first on the frame's buffers (32-bit tile ids in the
+    key buffers' front halves); returns (image, M, sorted tile ids, values)."""
+    s = fr.scene
+    out = torch.zeros((cam.height, cam.width, 3), dtype=torch.uint8, device=fr.dev)
+    f3 = (ctypes.c_float * 3)
+    tu, ts = fr.ku.view(torch.int32), fr.ks.view(torch.int32)
+    st = lib().gsr_forward_depth_first(
+        variant, s.num_vertex, s.position.data_ptr(), s.shs_half.data_ptr(), 1, s.opacity.data_ptr(),
+        s.cov3d.data_ptr(), cam.width, cam.height, 16, 16, f3(*cam.position.tolist()),
+        (ctypes.c_float * 9)(*cam.rotation.reshape(-1).tolist()), cam.focal_x, cam.focal_y, cam.zFar, cam.zNear,
+        fr.ctr.data_ptr(), fr.ws.data_ptr(), fr.ws.numel(), scratch.data_ptr(), scratch.numel(), tu.data_ptr(),
+        fr.vu.data_ptr(), ts.data_ptr(), fr.vs.data_ptr(), fr.cap, fr.xy.data_ptr(), fr.rgbd.data_ptr(),
+        fr.con.data_ptr(), fr.ranges.data_ptr(), f3(0.0, 0.0, 0.0), out.data_ptr(),
+        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    check(st, "forward_depth_first")
+    n = ctypes.c_int32(0)
+    check(lib().gsr_read_status(ctypes.c_void_p(fr.ws.data_ptr()), ctypes.c_void_p(fr.ctr.data_ptr()), fr.cap,
+                                ctypes.byref(n), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+          "read_status")
+    M = n.value
+    return out, M, ts[:M].cpu().numpy().view(np.uint32).copy(), fr.vs[:M].cpu().numpy().view(np.uint32).copy()
+
+
+@pytest.mark.parametrize("name,raw,spec", _cases(), ids=[c[0] for c in _cases()])
+def test_depth_first_quads_equal_single_pass_quads(cuda_device, name, raw, spec):
+    """The depth-first forward with quad keys: the same quad pairs as the
+    single-pass quad emission (expanded to exactly the per-tile triples), in
+    quad order, and the per-tile pipeline's image."""
+    scene = Scene.from_raw(raw, cuda_device)
+    cam = Camera.from_spec(spec)
+    fr = _Frame(scene, 8_000_000, cuda_device)
+    scratch = torch.zeros(lib().gsr_depth_first_scratch_size(scene.num_vertex), dtype=torch.int8, device=cuda_device)
+    gx = (cam.width + 15) // 16
+    img_t, kt, vt, _ = fr.forward(cam, R.RENDER_PERSISTENT_FUSED)
+    img_t = img_t.clone()
+    _, kq, _, _ = fr.forward(cam, R.RENDER_PERSISTENT_FUSED | QUAD)
+    # stale pairs in the buffers must not matter: fill them first
+    fr.ku.fill_(-7)
+    fr.ks.fill_(-7)
+    fr.vu.fill_(-7)
+    fr.vs.fill_(-7)
+    img_d, M, tiles, vals = _depth_first(fr, cam, R.RENDER_PERSISTENT_FUSED | QUAD, scratch)
+    assert M == len(kq), (M, len(kq))
+    assert torch.equal(img_d, img_t), int((img_d != img_t).sum())
+    assert np.all(np.diff(tiles.astype(np.int64)) >= 0)
+    depth = (kt & np.uint64(0xFFFFFFFF)).astype(np.int64)
+    by_gid = dict(zip(vt.tolist(), depth.tolist()))
+    keys = (tiles.astype(np.uint64) << np.uint64(32)) | np.array(
+        [by_gid[int(v & ((1 << 28) - 1))] for v in vals], dtype=np.uint64)
+    assert np.array_equal(_sorted_rows(_expand_quads(keys, vals, gx)), _sorted_rows(_per_tile(kt, vt)))
+
+
 def test_batched_quads_equal_single_view_per_tile_images(cuda_device):
     """Several views through the batcher with quad keys, and the emission
     thresholds lowered so that most rectangles take the large-Gaussian queue

@@ -82,3 +82,15 @@ def test_key_estimator_splits_a_batch_count_by_estimate():
     ea, eb = est(0, a), est(1, b)
     est.observe_batch([(0, a), (1, b)], 10 * (ea + eb))
     assert est(0, a) >= 9 * ea and est(1, b) >= 9 * eb
+
+
+def test_quad_key_tiles():
+    """With quad keys a view's key tile ids are its 2 x 2 groups of 16 x 16
+    tiles: ceil(W / 32) x ceil(H / 32)."""
+    cfg = TuneConfig(quad=True)
+    assert cfg.key_tiles(1920, 1080) == 60 * 34
+    assert cfg.key_tiles(3840, 2160) == 120 * 68
+    assert cfg.key_tiles(1000, 584) == 32 * 19  # 63 x 37 tiles
+    assert TuneConfig().key_tiles(1920, 1080) == 120 * 68
+    assert cfg.batch_variant() & 0x100 and not TuneConfig().batch_variant() & 0x100
+
