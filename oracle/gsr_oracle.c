@@ -566,7 +566,8 @@ void ora_render(int64_t n, const uint32_t* vals, const int32_t* ranges, const fl
  * differences of it check the gradients of the CUDA backward.  Tiles are
  * rendered by nthreads threads; the result does not depend on the count. */
 typedef struct {
-    double px, py, depth, con[3], log2o, rgb[3];
+    double px, py, depth, con[3], log2o, rgb[3], power;
+    int x0, y0, x1, y1;  /* tile rectangle */
     int ok;
 } ora_dg;
 
@@ -630,19 +631,26 @@ static void* dimg_worker(void* arg)
     return NULL;
 }
 
-double ora_image_fp64(int P, const double* means, const double* log_scales, const double* quats,
-                      const double* logits, const double* shs, int W, int H, const float* cam_pos,
-                      const float* cam_rot, double fx, double fy, const double* bg, int cadence,
-                      const double* target, double* img, int nthreads)
+/* Per-Gaussian FP64 projection of the float-image path (scene transform,
+ * EWA conic, SH colour, tile rectangle), for Gaussians [P0, P1). */
+typedef struct {
+    const ora_cam* c;
+    int P0, P1, W, H, gx, gy;
+    double tanx, tany, fx, fy;
+    const double *means, *log_scales, *quats, *logits, *shs;
+    ora_dg* g;
+} ora_dproj_job;
+
+static void* dproj_worker(void* arg)
 {
-    ora_cam c;
-    make_cam(&c, W, H, cam_pos, cam_rot, fx, fy, 100.0, 0.01);
-    const int gx = (W + 15) / 16, gy = (H + 15) / 16, tiles = gx * gy;
-    const double tanx = W / (2.0 * fx), tany = H / (2.0 * fy);
-    ora_dg* g = (ora_dg*)calloc((size_t)(P > 0 ? P : 1), sizeof(ora_dg));
-    int64_t cap = 1024, n = 0;
-    ora_pair* pairs = (ora_pair*)malloc(sizeof(ora_pair) * cap);
-    for (int i = 0; i < P; i++) {
+    const ora_dproj_job* j = (const ora_dproj_job*)arg;
+    const ora_cam c = *j->c;
+    const int W = j->W, H = j->H, gx = j->gx, gy = j->gy;
+    const double tanx = j->tanx, tany = j->tany, fx = j->fx, fy = j->fy;
+    const double *means = j->means, *log_scales = j->log_scales, *quats = j->quats, *logits = j->logits,
+                 *shs = j->shs;
+    ora_dg* g = j->g;
+    for (int i = j->P0; i < j->P1; i++) {
         /* scene transform in double */
         double o = 1.0 / (1.0 + exp(-logits[i]));
         double s[3], q[4], qn = 0.0;
@@ -710,24 +718,80 @@ double ora_image_fp64(int P, const double* means, const double* log_scales, cons
             for (int k = 0; k < 16; k++) acc += B[k] * shs[48 * (size_t)i + 3 * k + ch];
             G->rgb[ch] = acc > 0.0 ? acc : 0.0;
         }
-        /* rectangle and tile test as the forward (centre rounded to float) */
+        /* tile rectangle as the forward (centre rounded to float) */
+        G->power = power;
+        double fpx = (float)G->px, fpy = (float)G->py;
+        G->x0 = imin(gx, imax(0, (int)((fpx - w) / 16)));
+        G->y0 = imin(gy, imax(0, (int)((fpy - h) / 16)));
+        G->x1 = imin(gx, imax(0, (int)((fpx + w) / 16) + 1));
+        G->y1 = imin(gy, imax(0, (int)((fpy + h) / 16) + 1));
+        G->ok = 1;
+    }
+    return NULL;
+}
+
+/* The float image of ora_image_fp64 on the tiles with tile_mask[t] != 0 only
+ * (every tile when tile_mask is NULL); the loss sums over those tiles'
+ * pixels.  rects_out (optional, [P][4]) receives each Gaussian's tile
+ * rectangle x0, y0, x1, y1 (all zero when culled).  A perturbation of one
+ * Gaussian changes only the tiles of its rectangle, so finite differences of
+ * the loss over those tiles equal those over the whole image. */
+double ora_image_fp64_masked(int P, const double* means, const double* log_scales, const double* quats,
+                             const double* logits, const double* shs, int W, int H, const float* cam_pos,
+                             const float* cam_rot, double fx, double fy, const double* bg, int cadence,
+                             const double* target, const uint8_t* tile_mask, int32_t* rects_out, double* img,
+                             int nthreads)
+{
+    ora_cam c;
+    make_cam(&c, W, H, cam_pos, cam_rot, fx, fy, 100.0, 0.01);
+    const int gx = (W + 15) / 16, gy = (H + 15) / 16, tiles = gx * gy;
+    const double tanx = W / (2.0 * fx), tany = H / (2.0 * fy);
+    ora_dg* g = (ora_dg*)calloc((size_t)(P > 0 ? P : 1), sizeof(ora_dg));
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    {
+        pthread_t pth[256];
+        ora_dproj_job pj[256];
+        const int per = (P + nthreads - 1) / nthreads;
+        for (int t = 0; t < nthreads; t++) {
+            ora_dproj_job* jb = &pj[t];
+            jb->c = &c; jb->W = W; jb->H = H; jb->gx = gx; jb->gy = gy;
+            jb->tanx = tanx; jb->tany = tany; jb->fx = fx; jb->fy = fy;
+            jb->means = means; jb->log_scales = log_scales; jb->quats = quats; jb->logits = logits; jb->shs = shs;
+            jb->g = g;
+            jb->P0 = imin(P, t * per);
+            jb->P1 = imin(P, (t + 1) * per);
+        }
+        for (int t = 1; t < nthreads; t++) pthread_create(&pth[t], NULL, dproj_worker, &pj[t]);
+        dproj_worker(&pj[0]);
+        for (int t = 1; t < nthreads; t++) pthread_join(pth[t], NULL);
+    }
+    int64_t cap = 1024, n = 0;
+    ora_pair* pairs = (ora_pair*)malloc(sizeof(ora_pair) * cap);
+    for (int i = 0; i < P; i++) {
+        const ora_dg* G = &g[i];
+        if (rects_out) {
+            rects_out[4 * (size_t)i + 0] = G->ok ? G->x0 : 0;
+            rects_out[4 * (size_t)i + 1] = G->ok ? G->y0 : 0;
+            rects_out[4 * (size_t)i + 2] = G->ok ? G->x1 : 0;
+            rects_out[4 * (size_t)i + 3] = G->ok ? G->y1 : 0;
+        }
+        if (!G->ok) continue;
         ora_geom tg;
         memset(&tg, 0, sizeof tg);
-        tg.px = G->px; tg.py = G->py; tg.power = power;
+        tg.px = G->px; tg.py = G->py; tg.power = G->power;
         tg.con[0] = G->con[0]; tg.con[1] = G->con[1]; tg.con[2] = G->con[2];
-        double fpx = (float)G->px, fpy = (float)G->py;
-        int x0 = imin(gx, imax(0, (int)((fpx - w) / 16))), y0 = imin(gy, imax(0, (int)((fpy - h) / 16)));
-        int x1 = imin(gx, imax(0, (int)((fpx + w) / 16) + 1)), y1 = imin(gy, imax(0, (int)((fpy + h) / 16) + 1));
-        for (int yy2 = y0; yy2 < y1; yy2++)
-            for (int xx2 = x0; xx2 < x1; xx2++) {
+        for (int yy2 = G->y0; yy2 < G->y1; yy2++)
+            for (int xx2 = G->x0; xx2 < G->x1; xx2++) {
+                const int t = yy2 * gx + xx2;
+                if (tile_mask && !tile_mask[t]) continue;
                 if (!tile_hit(&tg, xx2, yy2, 16, 16)) continue;
                 if (n == cap) { cap *= 2; pairs = (ora_pair*)realloc(pairs, sizeof(ora_pair) * cap); }
-                pairs[n].tile = (uint32_t)(yy2 * gx + xx2);
-                pairs[n].depth = tz;
+                pairs[n].tile = (uint32_t)t;
+                pairs[n].depth = G->depth;
                 pairs[n].gid = (uint32_t)i;
                 n++;
             }
-        G->ok = 1;
     }
     qsort(pairs, (size_t)n, sizeof(ora_pair), pair_cmp);
     int64_t* start = (int64_t*)calloc((size_t)tiles + 1, sizeof(int64_t));
@@ -748,6 +812,10 @@ double ora_image_fp64(int P, const double* means, const double* log_scales, cons
     double loss = 0.0;
     if (target)
         for (size_t k = 0; k < (size_t)W * H * 3; k++) {
+            if (tile_mask) {
+                const size_t px = k / 3;
+                if (!tile_mask[((int)(px / W) / 16) * gx + (int)(px % W) / 16]) continue;
+            }
             double d = img[k] - target[k];
             loss += d * d;
         }
@@ -755,4 +823,13 @@ double ora_image_fp64(int P, const double* means, const double* log_scales, cons
     free(pairs);
     free(g);
     return loss;
+}
+
+double ora_image_fp64(int P, const double* means, const double* log_scales, const double* quats,
+                      const double* logits, const double* shs, int W, int H, const float* cam_pos,
+                      const float* cam_rot, double fx, double fy, const double* bg, int cadence,
+                      const double* target, double* img, int nthreads)
+{
+    return ora_image_fp64_masked(P, means, log_scales, quats, logits, shs, W, H, cam_pos, cam_rot, fx, fy, bg,
+                                 cadence, target, NULL, NULL, img, nthreads);
 }

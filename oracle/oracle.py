@@ -60,6 +60,9 @@ def lib():
         L.ora_image_fp64.argtypes = [i32, P, P, P, P, P, i32, i32, P, P, ctypes.c_double, ctypes.c_double, P, i32, P,
                                      P, i32]
         L.ora_image_fp64.restype = ctypes.c_double
+        L.ora_image_fp64_masked.argtypes = [i32, P, P, P, P, P, i32, i32, P, P, ctypes.c_double, ctypes.c_double, P,
+                                            i32, P, P, P, P, i32]
+        L.ora_image_fp64_masked.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -246,3 +249,26 @@ def tile_order(ranges, x_blocks, morton_bucket=0, zigzag=0):
     ids = order[src].astype(np.int64)
     desc = np.stack([ids % x_blocks, ids // x_blocks, r[ids, 0], r[ids, 1]], axis=1).astype(np.int32)
     return order, key[order], t.astype(np.uint32), desc
+
+
+def image_fp64_masked(means, log_scales, quats, logits, shs, cam, tile_mask=None, bg=(0.0, 0.0, 0.0), cadence=8,
+                      target=None, nthreads=None):
+    """image_fp64 restricted to the 16x16 tiles where `tile_mask` (uint8
+    [tiles], row-major; None = every tile) is set: the loss sums over those
+    tiles' pixels only.  Returns (loss, image [H,W,3], rects [P,4]) with each
+    Gaussian's tile rectangle x0, y0, x1, y1 (zeros when culled)."""
+    f8 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    m, ls, q, lg, sh = f8(means), f8(log_scales), f8(quats), f8(logits), f8(shs).reshape(-1, 48)
+    P = lg.shape[0]
+    img = np.zeros((cam.height, cam.width, 3), np.float64)
+    rects = np.zeros((P, 4), np.int32)
+    cp, cr = _c(cam.position, np.float32).reshape(3), _c(cam.rotation, np.float32).reshape(9)
+    b = f8(bg).reshape(3)
+    tgt = f8(target) if target is not None else None
+    mask = np.ascontiguousarray(tile_mask, dtype=np.uint8) if tile_mask is not None else None
+    loss = lib().ora_image_fp64_masked(P, _p(m), _p(ls), _p(q), _p(lg), _p(sh), cam.width, cam.height, _p(cp),
+                                       _p(cr), float(cam.fx), float(cam.fy), _p(b), int(cadence),
+                                       _p(tgt) if tgt is not None else None, _p(mask) if mask is not None else None,
+                                       _p(rects), _p(img), nthreads or nthreads_default())
+    return float(loss), img, rects
+

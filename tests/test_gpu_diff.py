@@ -122,3 +122,74 @@ def test_gradients_config4_distribution(cuda_device):
     good = np.abs(gg - fd) <= 0.05 * np.abs(fd) + 0.01 * np.abs(fd).max()
     print("\nconfig-4 distribution: agree %d/64" % good.sum())
     assert good.sum() >= 60
+
+
+def test_gradients_config4_full_scene_tile_sampled(cuda_device):
+    """Config 4 at full size: 1 M Gaussians (means ~ N(0, 3^2 I)), 8 cameras
+    at 1280x720 on a radius-10 orbit, L2 loss against renders of the scene
+    with means perturbed by N(0, 0.05^2) and SH DC by N(0, 0.1^2).  The GPU
+    gradients are checked against FP64 central differences (h = 1e-4) of
+    the same loss on 64 sampled parameters.  A parameter of Gaussian g only
+    changes the tiles of g's rectangle, so each difference is evaluated by
+    the FP64 oracle on those tiles (grown by one tile) of every view that
+    sees g, which equals the whole image's difference
+    (tests/test_oracle.py::test_masked_fp64_loss_gives_the_whole_image_differences).
+    Same bar as above; every miss is printed and listed on failure."""
+    import math
+
+    raw = scenes.scene_plain_small(1_000_000, seed=4, mean_sigma=3.0)
+    specs = [scenes.orbit_camera(10.0, 2 * math.pi * k / 8, 0.0, 1280, 720, 900.0, id=k) for k in range(8)]
+    dev = cuda_device
+    rng = np.random.default_rng(4)
+    t = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float32, device=dev)
+    tm = raw.means + rng.normal(0, 0.05, raw.means.shape).astype(np.float32)
+    tsh = raw.shs.copy()
+    tsh[:, 0, :] += rng.normal(0, 0.1, tsh[:, 0, :].shape).astype(np.float32)
+    with torch.no_grad():
+        targets = [render(t(tm), t(raw.log_scales), t(raw.quats), t(raw.opacity_logits), t(tsh.reshape(-1, 48)),
+                          Camera.from_spec(c), key_capacity=1 << 24) for c in specs]
+    params = [t(a).requires_grad_(True) for a in (raw.means, raw.log_scales, raw.quats, raw.opacity_logits,
+                                                  raw.shs.reshape(-1, 48))]
+    loss = sum(((render(*params, Camera.from_spec(c), key_capacity=1 << 24) - tg) ** 2).sum()
+               for c, tg in zip(specs, targets))
+    loss.backward()
+    grads = [p.grad.detach().cpu().numpy().astype(np.float64) for p in params]
+    tnp = [tg.cpu().numpy().astype(np.float64) for tg in targets]
+    theta = [np.asarray(a, np.float64).copy() for a in (raw.means, raw.log_scales, raw.quats, raw.opacity_logits,
+                                                        raw.shs.reshape(-1, 48))]
+    # every Gaussian's tile rectangle in every view (FP64 projection)
+    rects = [O.image_fp64_masked(*theta, c, np.zeros(((720 + 15) // 16) * ((1280 + 15) // 16), np.uint8))[2]
+             for c in specs]
+    sel = np.random.default_rng(13)
+    gmag = np.abs(grads[0]).sum(1)
+    active = np.flatnonzero(gmag > 1e-3 * gmag.max())
+    picks = [(int(sel.choice(5, p=[0.25, 0.2, 0.2, 0.15, 0.2])), int(sel.choice(active))) for _ in range(64)]
+    picks = [(k, g, int(sel.integers(0, theta[k].shape[1])) if theta[k].ndim == 2 else 0) for k, g in picks]
+    gx, gy = (1280 + 15) // 16, (720 + 15) // 16
+    h = 1e-4
+    fd, gg = [], []
+    for k, g, j in picks:
+        idx = (g, j) if theta[k].ndim == 2 else (g,)
+        views = []
+        for v, r in enumerate(rects):
+            x0, y0, x1, y1 = (int(z) for z in r[g])
+            if x1 > x0 and y1 > y0:
+                m = np.zeros((gy, gx), np.uint8)
+                m[max(0, y0 - 1):min(gy, y1 + 1), max(0, x0 - 1):min(gx, x1 + 1)] = 1
+                views.append((v, m.reshape(-1)))
+        old = theta[k][idx]
+        lv = []
+        for sgn in (1.0, -1.0):
+            theta[k][idx] = old + sgn * h
+            lv.append(sum(O.image_fp64_masked(*theta, specs[v], m, target=tnp[v])[0] for v, m in views))
+        theta[k][idx] = old
+        fd.append((lv[0] - lv[1]) / (2 * h))
+        gg.append(grads[k][idx])
+    fd, gg = np.array(fd), np.array(gg)
+    good = np.abs(gg - fd) <= 0.05 * np.abs(fd) + 0.01 * np.abs(fd).max()
+    names = ["mean", "log_scale", "quat", "logit", "sh"]
+    misses = [(names[k], g, j, float(a), float(b)) for (k, g, j), a, b, ok in zip(picks, gg, fd, good) if not ok]
+    rel = np.abs(gg - fd) / (np.abs(fd) + 1e-12)
+    print("\nconfig 4, 1 M Gaussians, 8 x 1280x720: agree %d/64, median rel err %.2e; misses (param, gaussian, "
+          "index, gpu, fp64): %s" % (good.sum(), float(np.median(rel)), misses))
+    assert good.sum() >= 60, misses

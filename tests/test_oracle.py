@@ -179,3 +179,34 @@ def test_oracle_forward_deterministic_across_threads():
     b, pb = O.forward(sc.means, sc.shs, op, cov, cam, nthreads=5)
     np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(pa["keys_sorted"], pb["keys_sorted"])
+
+
+def test_masked_fp64_loss_gives_the_whole_image_differences():
+    """The tile-masked FP64 loss (used for finite differences on large scenes):
+    with every tile set it equals the whole-image loss bit for bit, and the
+    central difference of one Gaussian's parameter over the tiles of its
+    rectangle (grown by one tile) equals the whole image's."""
+    raw = scenes.scene_plain_small(600, seed=9, mean_sigma=1.2)
+    cam = scenes.orbit_camera(5.0, 0.4, 0.1, 160, 128, scenes.focal_for(160))
+    target = O.image_fp64(raw.means + 0.03, raw.log_scales, raw.quats, raw.opacity_logits, raw.shs, cam)[1]
+    full, img = O.image_fp64(raw.means, raw.log_scales, raw.quats, raw.opacity_logits, raw.shs, cam, target=target)
+    gx, gy = (cam.width + 15) // 16, (cam.height + 15) // 16
+    allm, imgm, rects = O.image_fp64_masked(raw.means, raw.log_scales, raw.quats, raw.opacity_logits, raw.shs,
+                                            cam, np.ones(gx * gy, np.uint8), target=target)
+    assert allm == full and np.array_equal(img, imgm)
+    g = int(np.argmax((rects[:, 2] - rects[:, 0]) * (rects[:, 3] - rects[:, 1])))
+    x0, y0, x1, y1 = rects[g]
+    mask = np.zeros((gy, gx), np.uint8)
+    mask[max(0, y0 - 1):min(gy, y1 + 1), max(0, x0 - 1):min(gx, x1 + 1)] = 1
+    h = 1e-4
+    means = raw.means.astype(np.float64)
+    d_full, d_mask = [], []
+    for sgn in (1, -1):
+        m = means.copy()
+        m[g, 0] += sgn * h
+        d_full.append(O.image_fp64(m, raw.log_scales, raw.quats, raw.opacity_logits, raw.shs, cam, target=target)[0])
+        d_mask.append(O.image_fp64_masked(m, raw.log_scales, raw.quats, raw.opacity_logits, raw.shs, cam,
+                                          mask.reshape(-1), target=target)[0])
+    fd_full = (d_full[0] - d_full[1]) / (2 * h)
+    fd_mask = (d_mask[0] - d_mask[1]) / (2 * h)
+    assert abs(fd_full - fd_mask) <= 1e-9 * max(1.0, abs(fd_full)), (fd_full, fd_mask)
