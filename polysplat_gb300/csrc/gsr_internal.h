@@ -148,7 +148,7 @@ static_assert(offsetof(WorkspaceHeader, mq_count) == kPreprocessRegionOffset &&
 // Massive-Gaussian queue capacity of a workspace (entries of 48 bytes); the
 // queue sits right after the header.  Gaussians beyond it are emitted in
 // place by their own warp (slower, same keys).
-constexpr int kMassiveQueueEntries = 1 << 18;
+constexpr int kMassiveQueueEntries = 1 << 20;  // 48 MB: a 4K view of a 10 M-Gaussian scene queues ~10^6
 constexpr int kMassiveHugeEntries = 1 << 15;
 constexpr size_t kMassiveQueueBytes = (size_t)kMassiveQueueEntries * sizeof(MassiveEntry);
 // Small workspace for preprocess-only and render-only calls.

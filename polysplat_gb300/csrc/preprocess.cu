@@ -422,6 +422,14 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
             point_valid = (rect_max.x - rect_min.x) * (rect_max.y - rect_min.y) > 0;
         } while (false);
     }
+    // The SH row is read only once the Gaussian has emitted, after the tile
+    // tests; fetching it into L2 now overlaps that DRAM latency with them.
+    if (!COUNT && point_valid) {
+        const char* row = reinterpret_cast<const char*>(a.shs) + (size_t)idx * (HALF ? 96 : 192);
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(row));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(row + (HALF ? 95 : 96)));
+        if (!HALF) asm volatile("prefetch.global.L2 [%0];" ::"l"(row + 191));
+    }
 
     Stage st{s_keys[COUNT ? 0 : warp], s_vals[COUNT ? 0 : warp], 0};
     const EmitOut out{a.keys, a.vals, a.cap, a.counter};

@@ -239,7 +239,9 @@ class Server:
         left = budget_bytes - large_slots * _LargeSlot.device_bytes(large_cap, max_P)
         tiles_4k = cfg.key_tiles(3840, 2160)
         max_g = min((1 << 31) - 1, cfg.max_views * max_P)
-        small_cap = 1 << 26
+        # 2^27 keys hold a 4K view of the largest served scene in quad keys,
+        # so such frames batch instead of taking the large lane
+        small_cap = 1 << 27
         while small_cap > (1 << 20) and small_slots * Batcher.device_bytes(cfg.max_views, small_cap, max_g,
                                                                           cfg.max_views * tiles_4k) > left:
             small_cap //= 2

@@ -68,6 +68,14 @@ class _Frame:
         return out, keys, vals, sk
 
 
+class _DevWords:
+    """int32 view of library-owned device words."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (int(ptr), False), "version": 3,
+                                         "strides": None}
+
+
 def _expand_quads(keys, vals, gx):
     """(tile, gaussian, depth) triples of quad keys, tile = y * gx + x."""
     qgx = (gx + 1) // 2
@@ -181,7 +189,7 @@ def test_batched_quads_equal_single_view_per_tile_images(cuda_device):
     """Several views through the batcher with quad keys, and the emission
     thresholds lowered so that most rectangles take the large-Gaussian queue
     and the queue overflows into the in-place sweep."""
-    raws = [scenes.subsample(scenes.scene_clustered(600_000, seed=1), 400_000, seed=4),
+    raws = [scenes.scene_clustered(3_000_000, seed=1),
             scenes.scene_clustered(50_000, seed=33),
             scenes.subsample(scenes.scene_plain_small(), 30_000, seed=1)]
     scs = [Scene.from_raw(r, cuda_device) for r in raws]
@@ -189,22 +197,30 @@ def test_batched_quads_equal_single_view_per_tile_images(cuda_device):
     views = [(0, scenes.camera_front(1920, 1080, 1400.0)),
              (1, scenes.orbit_camera(8.0, 0.7, 0.3, 1280, 720, f(1280))),
              (2, scenes.camera_front(800, 600, 600.0)),
-             (0, scenes.orbit_camera(9.0, 2.0, -0.2, 1000, 584, f(1000)))]
+             (0, scenes.orbit_camera(9.0, 2.0, -0.2, 1000, 584, f(1000))),
+             (0, scenes.orbit_camera(7.0, 3.5, 0.1, 1920, 1080, f(1920)))]
     bg = [0.1, 0.2, 0.3]
     singles = []
     for si, spec in views:
-        fr = _Frame(scs[si], 8_000_000, cuda_device)
+        fr = _Frame(scs[si], 16_000_000, cuda_device)
         img, _, _, _ = fr.forward(Camera.from_spec(spec), R.RENDER_PERSISTENT_FUSED, bg)
         singles.append(img.clone())
         del fr
     for thresholds in ((32, 2048), (2, 4)):
-        b = Batcher(8, 16_000_000, sum(scs[si].num_vertex for si, _ in views), 40_000, cuda_device)
+        b = Batcher(8, 24_000_000, sum(scs[si].num_vertex for si, _ in views), 40_000, cuda_device)
         b.set_thresholds(*thresholds)
         vs = [View(si, Camera.from_spec(spec), bg) for si, spec in views]
         b.render(scs, vs, variant=R.RENDER_PERSISTENT_FUSED | QUAD, half=True, use_graph=False)
         b.finish()
         for (si, spec), v, want in zip(views, vs, singles):
             assert torch.equal(v.out, want), (thresholds, spec.width, int((v.out != want).sum()))
+        if thresholds == (2, 4):
+            # word 3 of the workspace header counts the rectangles sent to
+            # the warp-swept region of the large-Gaussian queue (2^20 - 2^15
+            # slots; huge ones that found the CTA-swept region full come here
+            # too): past it, the in-place sweep ran
+            words = torch.as_tensor(_DevWords(lib().gsr_batcher_status(b._h), 4), device=cuda_device).cpu()
+            assert int(words[3]) > (1 << 20) - (1 << 15), words
         b.close()
 
 

@@ -4,8 +4,10 @@ computeCov3D (csrc/pybind.cpp:22-120), from tests/golden/host_reference.npz.
 
 The reference computes in FP32 on the CPU with the C library's exp; the
 device uses CUDA's fast-math exp and reciprocal square root, so the results
-agree to a few ulp, not bit for bit.  Bars: opacity within 4 ulp; every
-cov3d row within 4e-6 of its largest entry; positions and SH bit-exact.
+agree to a few ulp, not bit for bit.  Bars: opacity within a relative 2e-6
+(about 32 ulp: the fast-math exp's relative error grows with |logit|, and
+the edge rows reach logits of +-30); every cov3d row within 4e-6 of its
+largest entry; positions and SH bit-exact.
 """
 import os
 
@@ -21,8 +23,9 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "hos
 
 
 def _check(gold, op, cov):
-    ulp = np.abs(op.view(np.int32).astype(np.int64) - gold["ref_opacity"].view(np.int32).astype(np.int64))
-    assert ulp.max() <= 4, ulp.max()
+    ref = gold["ref_opacity"].astype(np.float64)
+    rel = np.abs(op.astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-38)
+    assert rel.max() <= 2e-6, (rel.max(), int(rel.argmax()))
     scale = np.abs(gold["ref_cov3d"]).max(axis=1, keepdims=True)
     err = np.abs(cov.astype(np.float64) - gold["ref_cov3d"]) / scale
     assert err.max() <= 4e-6, (err.max(), int(err.max(axis=1).argmax()))
