@@ -192,6 +192,7 @@ template <typename K>
 struct PassSmem {
     K keys[kSortTile];
     uint32_t vals[kSortTile];
+    uint8_t digs[kSortTile];            // each reordered key's digit, so the scatter need not recompute it
     uint32_t whist[kWarpsPerCta][256];  // per-warp digit counts, then warp-exclusive offsets
     uint32_t digit_excl[256];           // tile-local start of each digit
     int gofs[256];                      // global position of tile position 0 per digit
@@ -333,7 +334,8 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortJob<K> a, int pass
         }
         __syncthreads();
 
-        // ---- per-digit offsets: across warps, then across digits ----
+        // ---- per-digit offsets across warps; publish the tile's counts;
+        //      offsets across digits ----
         uint32_t dtot = 0;
         {
             const int d = threadIdx.x;
@@ -344,16 +346,34 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortJob<K> a, int pass
                     S.whist[w][d] = dtot;
                     dtot += c;
                 }
+                // later tiles' look-back can use the count before this tile's scan is done
+                st_relaxed_u32(look + (size_t)tile * 256 + d, (tile == 0 ? kFlagPrefix : kFlagAgg) | dtot);
             }
             const uint32_t ex = block_excl_scan(dtot, S.warp_sums);
             if (digit_thread) S.digit_excl[d] = ex;
         }
+        __syncthreads();  // digit_excl complete
+
+        // ---- reorder in shared memory: the warps without a digit do it while
+        //      the digit warps look back, and the digit warps after ----
+        auto reorder = [&]() {
+#pragma unroll
+            for (int i = 0; i < kSortItems; i++) {
+                const int o = wbase + i * 32 + (int)lane;
+                if (o < tcount) {
+                    const uint32_t pos = S.digit_excl[dig[i]] + S.whist[warp][dig[i]] + rank[i];
+                    S.keys[pos] = key[i];
+                    S.vals[pos] = val[i];
+                    S.digs[pos] = (uint8_t)dig[i];
+                }
+            }
+        };
+        if (!digit_thread) reorder();
 
         // ---- decoupled look-back: thread d owns digit d ----
         if (digit_thread) {
             const int d = threadIdx.x;
             uint32_t* my = look + (size_t)tile * 256 + d;
-            st_relaxed_u32(my, (tile == 0 ? kFlagPrefix : kFlagAgg) | dtot);
             // walk back four predecessors per round trip; stop at the first
             // inclusive prefix, re-reading any entry that is not published yet
             uint32_t excl = 0;
@@ -385,25 +405,15 @@ __global__ __launch_bounds__(kSortThreads, 2) void k_pass(SortJob<K> a, int pass
             }
             if (tile != 0) st_relaxed_u32(my, kFlagPrefix | ((excl + dtot) & kValueMask));
             S.gofs[d] = (int)(S.gstart[d] + excl) - (int)S.digit_excl[d];
+            reorder();
         }
         __syncthreads();
 
-        // ---- reorder in shared memory, then coalesced scatter ----
-#pragma unroll
-        for (int i = 0; i < kSortItems; i++) {
-            const int o = wbase + i * 32 + (int)lane;
-            if (o < tcount) {
-                const uint32_t pos = S.digit_excl[dig[i]] + S.whist[warp][dig[i]] + rank[i];
-                S.keys[pos] = key[i];
-                S.vals[pos] = val[i];
-            }
-        }
-        __syncthreads();
+        // ---- coalesced scatter of the digit runs ----
         bool oob = false;
         for (int p = threadIdx.x; p < tcount; p += kSortThreads) {
             const K k = S.keys[p];
-            const uint32_t d = (uint32_t)(order_word(k, km) >> shift) & ((1u << bits) - 1u);
-            const long long g = (long long)S.gofs[d] + p;
+            const long long g = (long long)S.gofs[S.digs[p]] + p;
             if (g < 0 || g >= n) {  // only after a look-back timeout: never write outside the buffer
                 oob = true;
                 continue;

@@ -37,7 +37,9 @@ def test_served_images_equal_alone(cuda_device, quad):
     request against the single-view 16x16 E2E forward."""
     raws, reqs = _mix(40, 1000.0)
     scs = [Scene.from_raw(r, cuda_device) for r in raws]
-    cfg = TuneConfig(max_views=6, large_keys=400_000, quad=quad)  # both lanes take work
+    # both lanes take work: a quad key stands for about 2.5 per-tile keys, so
+    # the large-lane threshold scales with the layout's key estimate
+    cfg = TuneConfig(max_views=6, large_keys=160_000 if quad else 400_000, quad=quad)
     srv = Server(scs, cuda_device, budget_bytes=6 << 30, config=cfg)
     st = srv.run(reqs, realtime=False)
     torch.cuda.synchronize()
