@@ -10,8 +10,6 @@
 // and keys are staged per warp in shared memory and flushed with one global
 // atomic per flush instead of one per 32-wide emission step.
 #include <algorithm>
-#include <cstdlib>
-#include <cstring>
 
 #include "gsr_internal.h"
 
@@ -707,19 +705,9 @@ constexpr int kMaxBandRows = 1024;  // tile rows of a CTA-swept rectangle that g
 // extent carries a few ulp of relative error.  Ill-conditioned ellipses
 // (det <= 1e-6 AC) and non-finite values get every tile of the rectangle
 // tested.
-//
-// Sure tiles.  A tile whose whole pixel box lies inside the ellipse passes
-// the exact test: the edge segment it tests lies inside the ellipse, so the
-// segment meets the root interval with room to spare.  The band also holds
-// the ellipse shrunk to w (1 - tau_i), tau_i = 256 u (1 + kappa) + 2e-4 (four
-// times the candidate bands' allowance for the test's rounding, plus a
-// relative margin); a box inside the shrunk ellipse by a further mi =
-// 1 + 2e-4 max(dxmax, dymax) pixels on every side is sure, and skips the
-// test.  Ellipses with kappa >= 1000 have no sure tiles.
 struct Band {
     float B, inv_a, det, dymax, dxmax, dyr, cx, cy, m;
-    float dymax_i, mi;  // the shrunk ellipse's half-height, and the sure tiles' pixel margin
-    bool ok, ok_i;
+    bool ok;
 };
 
 __device__ __forceinline__ Band make_band(float3 q, float power, float2 c)
@@ -741,10 +729,6 @@ __device__ __forceinline__ Band make_band(float3 q, float power, float2 c)
     b.m = 0.5f + 1e-5f * fmaxf(b.dxmax, b.dymax);
     b.ok = A > 0.0f && C > 0.0f && w > 0.0f && det > 1e-6f * (A * C) && b.dymax < 1e6f && b.dxmax < 1e6f &&
            fabsf(b.dyr) < 1e6f && fabsf(c.x) < 1e7f && fabsf(c.y) < 1e7f;
-    const float wi = w * (1.0f - (256.0f * 5.9604645e-8f * (1.0f + kappa) + 2e-4f));
-    b.dymax_i = sqrtf(fmaxf(0.0f, wi) * A / det);
-    b.mi = 1.0f + 2e-4f * fmaxf(b.dxmax, b.dymax);
-    b.ok_i = b.ok && kappa < 1000.0f && wi > 0.0f && b.dymax_i < b.dymax;
     return b;
 }
 
@@ -770,95 +754,11 @@ __device__ __forceinline__ bool band_columns(const Band& e, int ty, int by, int 
     return c_lo <= c_hi;
 }
 
-// Sure columns [s_lo, s_hi] of tile row `ty` within its candidate columns
-// [c_lo, c_hi] (empty: s_lo > s_hi): tiles whose pixel box lies inside the
-// shrunk ellipse by mi pixels.  The ellipse's left edge is convex in dy and
-// its right edge concave, so over the row's pixel band [p, q] the inner
-// extent is set at p or q.
-__device__ __forceinline__ void band_sure(const Band& e, int ty, int by, int bx, int c_lo, int c_hi, int& s_lo,
-                                          int& s_hi)
-{
-    s_lo = 0;
-    s_hi = -1;
-    if (!e.ok_i) return;
-    const float p = (float)(ty * by) - e.cy, q = (float)(ty * by + by - 1) - e.cy;
-    if (!(p >= -e.dymax_i && q <= e.dymax_i)) return;
-    auto half = [&](float dy) {
-        return sqrtf(e.det * fmaxf(0.0f, e.dymax_i - dy) * fmaxf(0.0f, e.dymax_i + dy)) * e.inv_a;
-    };
-    const float hp = half(p), hq = half(q);
-    const float mp = -e.B * p * e.inv_a, mq = -e.B * q * e.inv_a;
-    const float xl = fmaxf(mp - hp, mq - hq), xr = fminf(mp + hp, mq + hq);
-    // the box [x bx, x bx + bx - 1] inside [cx + xl + mi, cx + xr - mi]
-    const float lo = ceilf((e.cx + xl + e.mi) / (float)bx);
-    const float hi = floorf((e.cx + xr - e.mi - (float)(bx - 1)) / (float)bx);
-    if (!(lo <= hi) || !(lo <= (float)c_hi) || !(hi >= (float)c_lo)) return;  // also rejects NaN
-    s_lo = (int)fmaxf((float)c_lo, lo);
-    s_hi = (int)fminf((float)c_hi, hi);
-}
-
-// One row of candidate columns [clo, chi] with its sure run [slo, shi] (a
-// sub-range, or empty): the columns around the sure run (left run from clo,
-// right run from shi + 1) 32 at a time with the exact test, then the sure run
-// 32 at a time without it.  step(valid, x, y, sure) is called by all lanes
-// together; `sure` is the same for every lane of a call.
-template <typename F>
-__device__ __forceinline__ void sweep_row(unsigned lane, int y, int clo, int chi, int slo, int shi, F&& step)
-{
-    const int nc = chi >= clo ? chi - clo + 1 : 0;
-    const int ns = slo <= shi ? shi - slo + 1 : 0;
-    const int nl = ns ? slo - clo : nc, nt = nc - ns;
-    for (int t0 = 0; t0 < nt; t0 += 32) {
-        const int t = t0 + (int)lane;
-        step(t < nt, t < nl ? clo + t : shi + 1 + (t - nl), y, false);
-    }
-    for (int x0 = slo; x0 <= shi; x0 += 32) step(x0 + (int)lane <= shi, x0 + (int)lane, y, true);
-}
-
-// The same for the 32 rows r0 + lane of a warp, each lane holding its row's
-// columns: the tested columns of all rows form one flattened task list and
-// the sure runs another, 32 tasks per call of step.
-template <typename F>
-__device__ __forceinline__ void sweep_rows(int r0, unsigned lane, int clo, int chi, int slo, int shi, F&& step)
-{
-    const int nc = chi >= clo ? chi - clo + 1 : 0;
-    const int ns = slo <= shi ? shi - slo + 1 : 0;
-    const int nl = ns ? slo - clo : nc;
-#pragma unroll 1
-    for (int list = 0; list < 2; list++) {  // 0: tested columns, 1: sure runs
-        const int n = list ? ns : nc - ns;
-        int pref = n;  // inclusive prefix of the task counts
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int t = __shfl_up_sync(GSR_FULL_MASK, pref, d);
-            if ((int)lane >= d) pref += t;
-        }
-        const int total = __shfl_sync(GSR_FULL_MASK, pref, 31);
-        for (int base = 0; base < total; base += 32) {
-            const int task = base + (int)lane;
-            // owner row = first lane whose inclusive prefix exceeds the task
-            int lo = 0, hi = 31;
-#pragma unroll
-            for (int step_ = 0; step_ < 5; step_++) {
-                const int mid = (lo + hi) >> 1;
-                if (__shfl_sync(GSR_FULL_MASK, pref, mid) > task) hi = mid;
-                else lo = mid + 1;
-            }
-            const int t = task - (__shfl_sync(GSR_FULL_MASK, pref, lo) - __shfl_sync(GSR_FULL_MASK, n, lo));
-            const int o_clo = __shfl_sync(GSR_FULL_MASK, clo, lo), o_nl = __shfl_sync(GSR_FULL_MASK, nl, lo);
-            const int o_slo = __shfl_sync(GSR_FULL_MASK, slo, lo), o_shi = __shfl_sync(GSR_FULL_MASK, shi, lo);
-            const int x = list ? o_slo + t : (t < o_nl ? o_clo + t : o_shi + 1 + (t - o_nl));
-            step(task < total, x, r0 + lo, list != 0);
-        }
-    }
-}
-
 // Sweep the tiles of one huge queued Gaussian with the whole CTA; on_step(v,
-// x, y) is called by every lane of a warp together, v = the tile's exact test
-// (true without the test for sure tiles, when `sure` is set).
+// x, y) is called by every lane of a warp together, v = the tile's exact test.
 template <typename F>
-__device__ __forceinline__ void sweep_cta(const MassiveEntry& me, const PreprocessParams& a, short4* s_band,
-                                          unsigned lane, int warp, bool sure, F&& on_step)
+__device__ __forceinline__ void sweep_cta(const MassiveEntry& me, const PreprocessParams& a, short2* s_band,
+                                          unsigned lane, int warp, F&& on_step)
 {
     const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
     const float pw = me.ctr_power_depth.z;
@@ -869,21 +769,22 @@ __device__ __forceinline__ void sweep_cta(const MassiveEntry& me, const Preproce
     const Band eb = make_band(q, pw, c);
     if (eb.ok && (y_hi - y_lo) <= kMaxBandRows) {
         for (int r = threadIdx.x; r < y_hi - y_lo; r += kThreads) {
-            int clo = 0, chi = -1, slo = 0, shi = -1;
+            int clo = 0, chi = -1;
             if (!band_columns(eb, y_lo + r, a.by, a.bx, x_lo, x_hi, clo, chi)) {
                 clo = 0;
                 chi = -1;
-            } else if (sure) {
-                band_sure(eb, y_lo + r, a.by, a.bx, clo, chi, slo, shi);
             }
-            s_band[r] = make_short4((short)clo, (short)chi, (short)slo, (short)shi);
+            s_band[r] = make_short2((short)clo, (short)chi);
         }
         __syncthreads();
         for (int r = warp; r < y_hi - y_lo; r += kWarps) {
-            const short4 b = s_band[r];
-            sweep_row(lane, y_lo + r, b.x, b.y, b.z, b.w, [&](bool valid, int x, int y, bool is_sure) {
-                on_step(valid && (is_sure || tile_hit(x, y, a.bx, a.by, c, q, pw)), x, y);
-            });
+            const short2 band = s_band[r];
+            const int y = y_lo + r;
+            for (int x0 = band.x; x0 <= band.y; x0 += 32) {
+                const int x = x0 + (int)lane;
+                const bool v = x <= band.y && tile_hit(x, y, a.bx, a.by, c, q, pw);
+                on_step(v, x, y);
+            }
         }
         __syncthreads();  // s_band and on_step's shared counters are reused by the next entry
         return;
@@ -911,11 +812,10 @@ __device__ __forceinline__ void sweep_cta(const MassiveEntry& me, const Preproce
 }
 
 // Sweep the tiles of one large queued Gaussian with one warp: the candidate
-// tiles of 32 rows at a time form flattened task lists (sweep_rows), 32 per
-// step.
+// tiles of 32 rows at a time form one flattened task list, 32 tests per step.
 template <typename F>
 __device__ __forceinline__ void sweep_warp(const MassiveEntry& me, const PreprocessParams& a, unsigned lane,
-                                           bool sure, F&& on_step)
+                                           F&& on_step)
 {
     const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
     const float pw = me.ctr_power_depth.z;
@@ -925,16 +825,36 @@ __device__ __forceinline__ void sweep_warp(const MassiveEntry& me, const Preproc
     if (eb.ok) {
         for (int r0 = y_lo; r0 < y_hi; r0 += 32) {
             const int y = r0 + (int)lane;
-            int clo = 0, chi = -1, slo = 0, shi = -1;
-            if (y >= y_hi || !band_columns(eb, y, a.by, a.bx, x_lo, x_hi, clo, chi)) {
-                clo = 0;
-                chi = -1;
-            } else if (sure) {
-                band_sure(eb, y, a.by, a.bx, clo, chi, slo, shi);
+            int clo = 0, n = 0;
+            if (y < y_hi) {
+                int chi = -1;
+                if (band_columns(eb, y, a.by, a.bx, x_lo, x_hi, clo, chi)) n = chi - clo + 1;
             }
-            sweep_rows(r0, lane, clo, chi, slo, shi, [&](bool valid, int x, int yy, bool is_sure) {
-                on_step(valid && (is_sure || tile_hit(x, yy, a.bx, a.by, c, q, pw)), x, yy);
-            });
+            int pref = n;  // inclusive prefix of the candidate counts
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int t = __shfl_up_sync(GSR_FULL_MASK, pref, d);
+                if ((int)lane >= d) pref += t;
+            }
+            const int total = __shfl_sync(GSR_FULL_MASK, pref, 31);
+            for (int base = 0; base < total; base += 32) {
+                const int task = base + (int)lane;
+                // owner row = first lane whose inclusive prefix exceeds the task
+                int lo = 0, hi = 31;
+#pragma unroll
+                for (int step = 0; step < 5; step++) {
+                    const int mid = (lo + hi) >> 1;
+                    if (__shfl_sync(GSR_FULL_MASK, pref, mid) > task) hi = mid;
+                    else lo = mid + 1;
+                }
+                const int o_pref = __shfl_sync(GSR_FULL_MASK, pref, lo);
+                const int o_n = __shfl_sync(GSR_FULL_MASK, n, lo);
+                const int o_clo = __shfl_sync(GSR_FULL_MASK, clo, lo);
+                const int x = o_clo + task - (o_pref - o_n);
+                const int yy = r0 + lo;
+                const bool v = task < total && tile_hit(x, yy, a.bx, a.by, c, q, pw);
+                on_step(v, x, yy);
+            }
         }
         return;
     }
@@ -956,15 +876,10 @@ __device__ __forceinline__ void sweep_warp(const MassiveEntry& me, const Preproc
 
 // Candidate quad columns [q_lo, q_hi] of quad row `qy`: the union of the
 // candidate tile columns of its (one or two) tile rows inside [y_lo, y_hi).
-// With `sure`, also the sure quads [s_lo, s_hi] (empty: s_lo > s_hi): both
-// tile rows inside [y_lo, y_hi) and all four tiles sure, so the quad's mask
-// is full.
 __device__ __forceinline__ bool band_quads(const Band& e, int qy, int by, int bx, int x_lo, int x_hi, int y_lo,
-                                           int y_hi, bool sure, int& q_lo, int& q_hi, int& s_lo, int& s_hi)
+                                           int y_hi, int& q_lo, int& q_hi)
 {
     int lo = 0x7FFFFFFF, hi = -1;
-    int slo = 0, shi = 0x7FFFFFFF;
-    bool all_sure = sure;
 #pragma unroll
     for (int s = 0; s < 2; s++) {
         const int ty = 2 * qy + s;
@@ -972,25 +887,10 @@ __device__ __forceinline__ bool band_quads(const Band& e, int qy, int by, int bx
         if (ty >= y_lo && ty < y_hi && band_columns(e, ty, by, bx, x_lo, x_hi, clo, chi)) {
             lo = min(lo, clo);
             hi = max(hi, chi);
-            if (all_sure) {
-                int a = 0, b = -1;
-                band_sure(e, ty, by, bx, clo, chi, a, b);
-                if (a > b) all_sure = false;
-                slo = max(slo, a);
-                shi = min(shi, b);
-            }
-        } else {
-            all_sure = false;
         }
     }
     q_lo = lo >> 1;
     q_hi = hi >> 1;
-    s_lo = 0;
-    s_hi = -1;
-    if (all_sure && slo <= shi) {
-        s_lo = max((slo + 1) >> 1, q_lo);  // 2 qx >= slo
-        s_hi = min((shi - 1) >> 1, q_hi);  // 2 qx + 1 <= shi
-    }
     return hi >= lo;
 }
 
@@ -998,8 +898,8 @@ __device__ __forceinline__ bool band_quads(const Band& e, int qy, int by, int bx
 // the quad and v = mask != 0.  A tile that passes the exact test lies in its
 // row's band, so its quad lies in the quad row's band.
 template <typename F>
-__device__ __forceinline__ void sweep_cta_quad(const MassiveEntry& me, const PreprocessParams& a, short4* s_band,
-                                               unsigned lane, int warp, bool sure, F&& on_step)
+__device__ __forceinline__ void sweep_cta_quad(const MassiveEntry& me, const PreprocessParams& a, short2* s_band,
+                                               unsigned lane, int warp, F&& on_step)
 {
     const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
     const float pw = me.ctr_power_depth.z;
@@ -1010,23 +910,22 @@ __device__ __forceinline__ void sweep_cta_quad(const MassiveEntry& me, const Pre
     const Band eb = make_band(q, pw, c);
     if (eb.ok && (qy_hi - qy_lo) <= kMaxBandRows) {
         for (int r = threadIdx.x; r < qy_hi - qy_lo; r += kThreads) {
-            int lo = 0, hi = -1, slo = 0, shi = -1;
-            if (!band_quads(eb, qy_lo + r, a.by, a.bx, x_lo, x_hi, y_lo, y_hi, sure, lo, hi, slo, shi)) {
+            int lo = 0, hi = -1;
+            if (!band_quads(eb, qy_lo + r, a.by, a.bx, x_lo, x_hi, y_lo, y_hi, lo, hi)) {
                 lo = 0;
                 hi = -1;
-                slo = 0;
-                shi = -1;
             }
-            s_band[r] = make_short4((short)lo, (short)hi, (short)slo, (short)shi);
+            s_band[r] = make_short2((short)lo, (short)hi);
         }
         __syncthreads();
         for (int r = warp; r < qy_hi - qy_lo; r += kWarps) {
-            const short4 b = s_band[r];
-            sweep_row(lane, qy_lo + r, b.x, b.y, b.z, b.w, [&](bool valid, int qx, int qy, bool is_sure) {
-                const uint32_t m =
-                    valid ? (is_sure ? 0xFu : quad_mask(qx, qy, rmin, rmax, a.bx, a.by, c, q, pw)) : 0u;
+            const short2 band = s_band[r];
+            const int qy = qy_lo + r;
+            for (int x0 = band.x; x0 <= band.y; x0 += 32) {
+                const int qx = x0 + (int)lane;
+                const uint32_t m = qx <= band.y ? quad_mask(qx, qy, rmin, rmax, a.bx, a.by, c, q, pw) : 0u;
                 on_step(m != 0u, qx, qy, m);
-            });
+            }
         }
         __syncthreads();
         return;
@@ -1055,7 +954,7 @@ __device__ __forceinline__ void sweep_cta_quad(const MassiveEntry& me, const Pre
 // sweep_warp over quads (see sweep_cta_quad).
 template <typename F>
 __device__ __forceinline__ void sweep_warp_quad(const MassiveEntry& me, const PreprocessParams& a, unsigned lane,
-                                                bool sure, F&& on_step)
+                                                F&& on_step)
 {
     const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
     const float pw = me.ctr_power_depth.z;
@@ -1067,18 +966,35 @@ __device__ __forceinline__ void sweep_warp_quad(const MassiveEntry& me, const Pr
     if (eb.ok) {
         for (int r0 = qy_lo; r0 < qy_hi; r0 += 32) {
             const int qy = r0 + (int)lane;
-            int clo = 0, chi = -1, slo = 0, shi = -1;
-            if (qy >= qy_hi || !band_quads(eb, qy, a.by, a.bx, x_lo, x_hi, y_lo, y_hi, sure, clo, chi, slo, shi)) {
-                clo = 0;
-                chi = -1;
-                slo = 0;
-                shi = -1;
+            int clo = 0, n = 0;
+            if (qy < qy_hi) {
+                int chi = -1;
+                if (band_quads(eb, qy, a.by, a.bx, x_lo, x_hi, y_lo, y_hi, clo, chi)) n = chi - clo + 1;
             }
-            sweep_rows(r0, lane, clo, chi, slo, shi, [&](bool valid, int qx, int qyy, bool is_sure) {
-                const uint32_t m =
-                    valid ? (is_sure ? 0xFu : quad_mask(qx, qyy, rmin, rmax, a.bx, a.by, c, q, pw)) : 0u;
+            int pref = n;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int t = __shfl_up_sync(GSR_FULL_MASK, pref, d);
+                if ((int)lane >= d) pref += t;
+            }
+            const int total = __shfl_sync(GSR_FULL_MASK, pref, 31);
+            for (int base = 0; base < total; base += 32) {
+                const int task = base + (int)lane;
+                int lo = 0, hi = 31;
+#pragma unroll
+                for (int step = 0; step < 5; step++) {
+                    const int mid = (lo + hi) >> 1;
+                    if (__shfl_sync(GSR_FULL_MASK, pref, mid) > task) hi = mid;
+                    else lo = mid + 1;
+                }
+                const int o_pref = __shfl_sync(GSR_FULL_MASK, pref, lo);
+                const int o_n = __shfl_sync(GSR_FULL_MASK, n, lo);
+                const int o_clo = __shfl_sync(GSR_FULL_MASK, clo, lo);
+                const int qx = o_clo + task - (o_pref - o_n);
+                const int qyy = r0 + lo;
+                const uint32_t m = task < total ? quad_mask(qx, qyy, rmin, rmax, a.bx, a.by, c, q, pw) : 0u;
                 on_step(m != 0u, qx, qyy, m);
-            });
+            }
         }
         return;
     }
@@ -1118,8 +1034,7 @@ enum : int { kMassiveEmit64 = 0, kMassiveCount = 1, kMassiveEmitDf = 2 };
 // whose mask is not empty counts as one, and is written as (quad id, index |
 // mask << kQuadShift).
 template <int MODE, bool VIEWS, bool QUAD = false>
-__global__ __launch_bounds__(kThreads, 3) void k_emit_massive(const __grid_constant__ PreprocessParams a, const DfEmit df,
-                                                           const int sure)
+__global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant__ PreprocessParams a, const DfEmit df)
 {
     __shared__ uint64_t s_keys[MODE == kMassiveEmit64 ? kWarps : 1][kStage];
     __shared__ uint32_t s_vals[MODE == kMassiveEmit64 ? kWarps : 1][kStage];
@@ -1128,7 +1043,7 @@ __global__ __launch_bounds__(kThreads, 3) void k_emit_massive(const __grid_const
     __shared__ int s_entry;
     __shared__ uint32_t s_pos;
     __shared__ uint32_t s_wcnt[kWarps];
-    __shared__ short4 s_band[kMaxBandRows];
+    __shared__ short2 s_band[kMaxBandRows];
     const unsigned lane = threadIdx.x & 31u;
     const int warp = threadIdx.x >> 5;
     Stage st{s_keys[MODE == kMassiveEmit64 ? warp : 0], s_vals[MODE == kMassiveEmit64 ? warp : 0], 0};
@@ -1154,23 +1069,23 @@ __global__ __launch_bounds__(kThreads, 3) void k_emit_massive(const __grid_const
         const PreprocessParams& av = VIEWS ? a.views[(uint32_t)me.rect.x >> 16] : a;
         if (MODE == kMassiveEmit64 && QUAD) {
             const int qgx = quad_cols(av.gx);
-            sweep_cta_quad(me, av, s_band, lane, warp, sure, [&](bool v, int qx, int qy, uint32_t m) {
+            sweep_cta_quad(me, av, s_band, lane, warp, [&](bool v, int qx, int qy, uint32_t m) {
                 uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + qy * qgx + qx) << 32) | db;
                 stage_emit(st, out, v, key, gid | (m << kQuadShift), lane);
             });
         } else if (MODE == kMassiveEmit64) {
-            sweep_cta(me, av, s_band, lane, warp, sure, [&](bool v, int x, int y) {
+            sweep_cta(me, av, s_band, lane, warp, [&](bool v, int x, int y) {
                 uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + y * av.gx + x) << 32) | db;
                 stage_emit(st, out, v, key, gid, lane);
             });
         } else if (MODE == kMassiveCount) {
             uint32_t cnt = 0;
             if (QUAD)
-                sweep_cta_quad(me, a, s_band, lane, warp, sure, [&](bool v, int, int, uint32_t) {
+                sweep_cta_quad(me, a, s_band, lane, warp, [&](bool v, int, int, uint32_t) {
                     cnt += __popc(__ballot_sync(GSR_FULL_MASK, v));
                 });
             else
-                sweep_cta(me, a, s_band, lane, warp, sure, [&](bool v, int, int) {
+                sweep_cta(me, a, s_band, lane, warp, [&](bool v, int, int) {
                     cnt += __popc(__ballot_sync(GSR_FULL_MASK, v));
                 });
             if (lane == 0) s_wcnt[warp] = cnt;
@@ -1200,11 +1115,11 @@ __global__ __launch_bounds__(kThreads, 3) void k_emit_massive(const __grid_const
             };
             if (QUAD) {
                 const int qgx = quad_cols(a.gx);
-                sweep_cta_quad(me, a, s_band, lane, warp, sure, [&](bool v, int qx, int qy, uint32_t m) {
+                sweep_cta_quad(me, a, s_band, lane, warp, [&](bool v, int qx, int qy, uint32_t m) {
                     put(v, (uint32_t)(qy * qgx + qx), gid | (m << kQuadShift));
                 });
             } else {
-                sweep_cta(me, a, s_band, lane, warp, sure,
+                sweep_cta(me, a, s_band, lane, warp,
                           [&](bool v, int x, int y) { put(v, (uint32_t)(y * a.gx + x), gid); });
             }
             // sweep_cta ended on a barrier, so s_pos is final; every thread
@@ -1232,22 +1147,22 @@ __global__ __launch_bounds__(kThreads, 3) void k_emit_massive(const __grid_const
         const PreprocessParams& av = VIEWS ? a.views[(uint32_t)me.rect.x >> 16] : a;
         if (MODE == kMassiveEmit64 && QUAD) {
             const int qgx = quad_cols(av.gx);
-            sweep_warp_quad(me, av, lane, sure, [&](bool v, int qx, int qy, uint32_t m) {
+            sweep_warp_quad(me, av, lane, [&](bool v, int qx, int qy, uint32_t m) {
                 uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + qy * qgx + qx) << 32) | db;
                 stage_emit(st, out, v, key, gid | (m << kQuadShift), lane);
             });
         } else if (MODE == kMassiveEmit64) {
-            sweep_warp(me, av, lane, sure, [&](bool v, int x, int y) {
+            sweep_warp(me, av, lane, [&](bool v, int x, int y) {
                 uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + y * av.gx + x) << 32) | db;
                 stage_emit(st, out, v, key, gid, lane);
             });
         } else if (MODE == kMassiveCount) {
             uint32_t cnt = 0;
             if (QUAD)
-                sweep_warp_quad(me, a, lane, sure,
+                sweep_warp_quad(me, a, lane,
                                 [&](bool v, int, int, uint32_t) { cnt += __popc(__ballot_sync(GSR_FULL_MASK, v)); });
             else
-                sweep_warp(me, a, lane, sure, [&](bool v, int, int) { cnt += __popc(__ballot_sync(GSR_FULL_MASK, v)); });
+                sweep_warp(me, a, lane, [&](bool v, int, int) { cnt += __popc(__ballot_sync(GSR_FULL_MASK, v)); });
             if (lane == 0) a.df.count[gid] = cnt;
         } else {
             const uint32_t count = a.df.count[gid];
@@ -1265,11 +1180,11 @@ __global__ __launch_bounds__(kThreads, 3) void k_emit_massive(const __grid_const
             };
             if (QUAD) {
                 const int qgx = quad_cols(a.gx);
-                sweep_warp_quad(me, a, lane, sure, [&](bool v, int qx, int qy, uint32_t m) {
+                sweep_warp_quad(me, a, lane, [&](bool v, int qx, int qy, uint32_t m) {
                     put(v, (uint32_t)(qy * qgx + qx), gid | (m << kQuadShift));
                 });
             } else {
-                sweep_warp(me, a, lane, sure, [&](bool v, int x, int y) { put(v, (uint32_t)(y * a.gx + x), gid); });
+                sweep_warp(me, a, lane, [&](bool v, int x, int y) { put(v, (uint32_t)(y * a.gx + x), gid); });
             }
             for (uint32_t k = wpos + lane; k < count; k += 32)
                 if (base + k < df.cap) {
@@ -1498,18 +1413,6 @@ cudaError_t launch_scene_prepare(int P, const float* log_scales, const float* qu
     return cudaGetLastError();
 }
 
-// 1 unless GSR_MASSIVE_SURE=0 (read once per process), which makes the
-// large-Gaussian sweeps run the exact test on sure tiles too.  Both settings
-// emit the same tiles; the switch exists so that can be checked.
-static int massive_sure()
-{
-    static const int on = [] {
-        const char* e = getenv("GSR_MASSIVE_SURE");
-        return (e && strcmp(e, "0") == 0) ? 0 : 1;
-    }();
-    return on;
-}
-
 // Persistent grid of the queue sweeps: as many CTAs as fit on every SM.
 template <typename Kern>
 static int emit_grid(Kern kern)
@@ -1548,12 +1451,12 @@ static cudaError_t preprocess_common(const PreprocessParams& p, bool half_sh, bo
     const DfEmit none{nullptr, nullptr, nullptr, nullptr, 0};
     if (count && p.quad)
         k_emit_massive<kMassiveCount, false, true>
-            <<<emit_grid(k_emit_massive<kMassiveCount, false, true>), kThreads, 0, stream>>>(p, none, massive_sure());
-    else if (count) k_emit_massive<kMassiveCount, false><<<emit_grid(k_emit_massive<kMassiveCount, false>), kThreads, 0, stream>>>(p, none, massive_sure());
+            <<<emit_grid(k_emit_massive<kMassiveCount, false, true>), kThreads, 0, stream>>>(p, none);
+    else if (count) k_emit_massive<kMassiveCount, false><<<emit_grid(k_emit_massive<kMassiveCount, false>), kThreads, 0, stream>>>(p, none);
     else if (p.quad)
         k_emit_massive<kMassiveEmit64, false, true>
-            <<<emit_grid(k_emit_massive<kMassiveEmit64, false, true>), kThreads, 0, stream>>>(p, none, massive_sure());
-    else k_emit_massive<kMassiveEmit64, false><<<emit_grid(k_emit_massive<kMassiveEmit64, false>), kThreads, 0, stream>>>(p, none, massive_sure());
+            <<<emit_grid(k_emit_massive<kMassiveEmit64, false, true>), kThreads, 0, stream>>>(p, none);
+    else k_emit_massive<kMassiveEmit64, false><<<emit_grid(k_emit_massive<kMassiveEmit64, false>), kThreads, 0, stream>>>(p, none);
     return cudaGetLastError();
 }
 
@@ -1573,13 +1476,13 @@ cudaError_t launch_preprocess_views(const PreprocessParams& base, int n_views, i
         else k_preprocess<false, false, true, true><<<grid, kThreads, 0, stream>>>(base);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         k_emit_massive<kMassiveEmit64, true, true>
-            <<<emit_grid(k_emit_massive<kMassiveEmit64, true, true>), kThreads, 0, stream>>>(base, none, massive_sure());
+            <<<emit_grid(k_emit_massive<kMassiveEmit64, true, true>), kThreads, 0, stream>>>(base, none);
         return cudaGetLastError();
     }
     if (half_sh) k_preprocess<true, false, true><<<grid, kThreads, 0, stream>>>(base);
     else k_preprocess<false, false, true><<<grid, kThreads, 0, stream>>>(base);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    k_emit_massive<kMassiveEmit64, true><<<emit_grid(k_emit_massive<kMassiveEmit64, true>), kThreads, 0, stream>>>(base, none, massive_sure());
+    k_emit_massive<kMassiveEmit64, true><<<emit_grid(k_emit_massive<kMassiveEmit64, true>), kThreads, 0, stream>>>(base, none);
     return cudaGetLastError();
 }
 
@@ -1602,10 +1505,10 @@ cudaError_t launch_df_emit_massive(const PreprocessParams& p, const uint32_t* of
     const DfEmit df{offsets, rank, tiles, vals, cap};
     if (p.quad)
         k_emit_massive<kMassiveEmitDf, false, true>
-            <<<emit_grid(k_emit_massive<kMassiveEmitDf, false, true>), kThreads, 0, stream>>>(p, df, massive_sure());
+            <<<emit_grid(k_emit_massive<kMassiveEmitDf, false, true>), kThreads, 0, stream>>>(p, df);
     else
         k_emit_massive<kMassiveEmitDf, false>
-            <<<emit_grid(k_emit_massive<kMassiveEmitDf, false>), kThreads, 0, stream>>>(p, df, massive_sure());
+            <<<emit_grid(k_emit_massive<kMassiveEmitDf, false>), kThreads, 0, stream>>>(p, df);
     return cudaGetLastError();
 }
 
@@ -1619,7 +1522,7 @@ __global__ __launch_bounds__(256) void k_es_pass_b(int P, int bx, int by, int gx
                                                    const int32_t* __restrict__ count_sorted,
                                                    const float2* __restrict__ xy, const float4* __restrict__ cpr,
                                                    const int2* __restrict__ rb, uint32_t* __restrict__ tiles,
-                                                   uint32_t* __restrict__ vals, long long cap, const int sure)
+                                                   uint32_t* __restrict__ vals, long long cap)
 {
     const unsigned lane = threadIdx.x & 31u;
     PreprocessParams pp;
@@ -1643,7 +1546,7 @@ __global__ __launch_bounds__(256) void k_es_pass_b(int P, int bx, int by, int gx
         const int x1 = min(gx, (int)(int16_t)(r.y & 0xFFFF)), y1 = (int)(int16_t)((r.y >> 16) & 0xFFFF);
         me.rect = make_int4(x0, max(x0, x1), y0, max(y0, y1));
         uint32_t wpos = 0;
-        sweep_warp(me, pp, lane, sure, [&](bool v, int x, int y) {
+        sweep_warp(me, pp, lane, [&](bool v, int x, int y) {
             const unsigned m = __ballot_sync(GSR_FULL_MASK, v);
             if (v) {
                 const long long pos = base + wpos + __popc(m & lanemask_lt());
@@ -1668,8 +1571,7 @@ cudaError_t launch_es_pass_b(int P, int bx, int by, int gx, const uint32_t* perm
 {
     if (P <= 0) return cudaSuccess;
     const int grid = std::min(div_up(P, 8), device_sm_count() * 8);
-    k_es_pass_b<<<grid, 256, 0, stream>>>(P, bx, by, gx, perm, cum, count_sorted, xy, cpr, rb, tiles, vals, cap,
-                                          massive_sure());
+    k_es_pass_b<<<grid, 256, 0, stream>>>(P, bx, by, gx, perm, cum, count_sorted, xy, cpr, rb, tiles, vals, cap);
     return cudaGetLastError();
 }
 

@@ -153,20 +153,6 @@ def scene_needles(n: int = 200_000, seed: int = 5) -> RawScene:
     return RawScene(means, log_scales, q, logits, shs)
 
 
-def scene_blobs(n: int = 4_000, seed: int = 9) -> RawScene:
-    """Test scene of large Gaussians close in front of camera_front: isotropic
-    to mildly elongated, scales from e^-2.5 to e^0.5 at 2 to 12 units from the
-    camera, so a 1080p view holds rectangles from tens of tiles up to the
-    whole image.  Exercises the large-Gaussian sweeps."""
-    rng = _rng(seed)
-    means = np.empty((n, 3), np.float32)
-    means[:, 2] = rng.uniform(-6.0, 4.0, n)
-    means[:, :2] = rng.normal(0.0, 1.0, (n, 2)) * (means[:, 2:] + 8.0) * 0.35
-    log_scales = rng.uniform(-2.5, 0.5, (n, 1)) + rng.uniform(-1.0, 0.0, (n, 3))
-    q, logits, shs = _common_attrs(rng, n)
-    return RawScene(means, log_scales.astype(np.float32), q, logits, shs)
-
-
 def scene_city(n: int = 20_000_000, seed: int = 2, n_clusters: int = 4096, per_cluster: int = 2000) -> RawScene:
     rng = _rng(seed)
     n_cl = min(n, n_clusters * per_cluster)
