@@ -4,15 +4,16 @@ No counterpart in the reference, which renders one view per call.  A server
 keeps several scenes resident on the device and renders a stream of
 requests (scene, camera, resolution) as they arrive.
 
-* Two lanes, on their own CUDA streams.
+* Two lanes; every buffer set of either lane has its own CUDA stream.
   - The small lane batches requests of modest key count and renders each
     batch with one pass of the pipeline (``Batcher``; a CUDA graph per batch
     shape, replayed).
   - The large lane renders one big request at a time with the depth-first
     forward, which sorts 32-bit tile ids in 2 passes instead of 64-bit keys
     in 5-6.
-  Small requests never queue behind a big one, and the work of both lanes
-  overlaps on the device.
+  Small requests never queue behind a big one, and the work of all buffer
+  sets overlaps on the device: one batch's sort and large-Gaussian sweeps
+  run beside the next batch's preprocess.
 * Admission is continuous: a request that arrives while others are on the
   GPU joins the next batch of its lane as soon as a buffer set of that lane
   is free.  Every buffer set is allocated once, at start-up, within the
@@ -251,9 +252,10 @@ class Server:
             b = Batcher(cfg.max_views, small_cap, max_g, cfg.max_views * tiles_4k, self.device)
             b.set_thresholds(cfg.massive_area, cfg.huge_area)
             ctr = _DevWord(b.counter_ptr(), "<i4", self.device).tensor()
+            # each slot has its own stream, so one batch's sort and sweeps
+            # overlap the next batch's preprocess on the device
             self.small.append({"b": b, "ctr": ctr, "host": torch.zeros(1, dtype=torch.int32, pin_memory=True),
-                               "event": torch.cuda.Event(), "job": None})
-        self.s_small = torch.cuda.Stream(self.device)
+                               "event": torch.cuda.Event(), "job": None, "stream": torch.cuda.Stream(self.device)})
         self.s_copy = torch.cuda.Stream(self.device)
         self.max_g = max_g
         self.tiles_cap = cfg.max_views * tiles_4k
@@ -322,16 +324,17 @@ class Server:
 
     def _launch_small(self, slot, reqs) -> None:
         views = []
-        with torch.cuda.stream(self.s_small):  # the caching allocator tracks the lane that writes it
+        stream = slot["stream"]
+        with torch.cuda.stream(stream):  # the caching allocator tracks the stream that writes it
             for r in reqs:
                 r.out = torch.empty((r.cam.height, r.cam.width, 3), dtype=torch.uint8, device=self.device)
                 views.append(View(r.scene, r.cam, self.bg, r.out))
         b = slot["b"]
         b.render(self.scenes, views, variant=self.cfg.batch_variant(), half=True, block_x=self.cfg.block_x,
-                 block_y=self.cfg.block_y, use_graph=True, stream=self.s_small)
-        with torch.cuda.stream(self.s_small):
+                 block_y=self.cfg.block_y, use_graph=True, stream=stream)
+        with torch.cuda.stream(stream):
             slot["host"].copy_(slot["ctr"], non_blocking=True)
-            slot["event"].record(self.s_small)
+            slot["event"].record(stream)
         self._deliver(reqs, slot["event"])
         slot["job"] = list(reqs)
 
@@ -465,11 +468,15 @@ class Server:
 # Gaussians a pixel blends after its tile saturates, and where a Gaussian's
 # conic is indefinite (alpha > 1) that changes the pixel by far more than
 # 2/255, so 32x16 and 32x32 tiles are not candidates.
+# max_batch_tiles stays at its default (2^14 key tiles).  A sequence of
+# candidates that ended with quad keys, 4 or 8 views per batch and a cap of
+# 2^13 or 2^15 tiles stopped with an illegal memory access (reproducible in
+# that order, not found by bounds checks on every global access); the cap is
+# not searched until the cause is found.
 DEFAULT_AXES = [("quad", [False, True]),
                 ("large_keys", [4_000_000, 16_000_000, 1 << 40]),
                 ("max_views", [4, 8, 16]),
-                (("massive_area", "huge_area"), [(64, 4096), (16, 1024)]),
-                ("max_batch_tiles", [1 << 13, 1 << 14, 1 << 15])]
+                (("massive_area", "huge_area"), [(64, 4096), (16, 1024)])]
 
 
 def autotune(scenes, sample_reqs, device, budget_bytes: int = 60 << 30, log=None, axes=None,
