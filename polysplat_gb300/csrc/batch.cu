@@ -263,7 +263,12 @@ gsr_batcher* gsr_batcher_create(int max_views, int64_t key_capacity, int64_t max
     b->d_views = reinterpret_cast<RenderView*>(take(s.views));
     b->counter = reinterpret_cast<int32_t*>(take(256));
     b->slot_bytes = al(s.pre) + al(s.views);
-    bool ok = cudaMemset(base, 0, s.total) == cudaSuccess &&
+    // The zero fill runs on the legacy default stream, which streams created
+    // non-blocking (every torch stream) do not wait for: it must be finished
+    // before any stream uses the block.  A batch launched on such a stream
+    // while the fill still ran had its parameter blocks cleared under it, and
+    // its kernels read null scene and image pointers.
+    bool ok = cudaMemset(base, 0, s.total) == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess &&
               cudaMallocHost(&b->h_stage, b->slot_bytes * kStagingSlots) == cudaSuccess;
     for (int i = 0; ok && i < kStagingSlots; i++)
         ok = cudaEventCreateWithFlags(&b->slot_done[i], cudaEventDisableTiming) == cudaSuccess;

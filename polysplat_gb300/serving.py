@@ -261,6 +261,9 @@ class Server:
         self.tiles_cap = cfg.max_views * tiles_4k
         self.deliver = False
         self._pinned: Dict[Tuple[int, int], List[torch.Tensor]] = collections.defaultdict(list)
+        # the large lane's buffers were zero-filled on the current stream; the
+        # lanes' own streams are non-blocking and would not wait for it
+        torch.cuda.synchronize(self.device)
 
     # -- delivery of results to host memory ------------------------------------------
     def _host_buffer(self, cam) -> torch.Tensor:
@@ -468,15 +471,11 @@ class Server:
 # Gaussians a pixel blends after its tile saturates, and where a Gaussian's
 # conic is indefinite (alpha > 1) that changes the pixel by far more than
 # 2/255, so 32x16 and 32x32 tiles are not candidates.
-# max_batch_tiles stays at its default (2^14 key tiles).  A sequence of
-# candidates that ended with quad keys, 4 or 8 views per batch and a cap of
-# 2^13 or 2^15 tiles stopped with an illegal memory access (reproducible in
-# that order, not found by bounds checks on every global access); the cap is
-# not searched until the cause is found.
 DEFAULT_AXES = [("quad", [False, True]),
                 ("large_keys", [4_000_000, 16_000_000, 1 << 40]),
                 ("max_views", [4, 8, 16]),
-                (("massive_area", "huge_area"), [(64, 4096), (16, 1024)])]
+                (("massive_area", "huge_area"), [(64, 4096), (16, 1024)]),
+                ("max_batch_tiles", [1 << 13, 1 << 14, 1 << 15])]
 
 
 def autotune(scenes, sample_reqs, device, budget_bytes: int = 60 << 30, log=None, axes=None,
