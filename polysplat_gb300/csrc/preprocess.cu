@@ -754,11 +754,68 @@ __device__ __forceinline__ bool band_columns(const Band& e, int ty, int by, int 
     return c_lo <= c_hi;
 }
 
+// The CTA's flattened sweep of `rows` rows of candidate columns (s_band[r] =
+// [lo, hi], empty when hi < lo): a block-wide prefix of the rows' counts
+// into s_pref, then each warp takes 32 consecutive candidates at a time, so
+// a narrow row shares a step with its neighbours instead of taking a step of
+// its own.  step(valid, x, r) is called by all lanes of a warp together.
+template <typename F>
+__device__ __forceinline__ void sweep_flat_cta(int rows, const short2* s_band, int* s_pref, int* s_wsum,
+                                               unsigned lane, int warp, F&& step)
+{
+    constexpr int kPer = kMaxBandRows / kThreads;  // rows per thread in the scan
+    const int r0 = (int)threadIdx.x * kPer;
+    int cnt[kPer];
+    int local = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const int r = r0 + k;
+        cnt[k] = r < rows ? max(0, (int)s_band[r].y - (int)s_band[r].x + 1) : 0;
+        local += cnt[k];
+    }
+    int incl = local;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(GSR_FULL_MASK, incl, d);
+        if ((int)lane >= d) incl += t;
+    }
+    if (lane == 31) s_wsum[warp] = incl;
+    __syncthreads();
+    int run = incl - local, total = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) {
+        if (w < warp) run += s_wsum[w];
+        total += s_wsum[w];
+    }
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        run += cnt[k];
+        if (r0 + k < rows) s_pref[r0 + k] = run;  // inclusive prefix of the rows' counts
+    }
+    __syncthreads();
+    for (int base = warp * 32; base < total; base += kWarps * 32) {
+        const int task = base + (int)lane;
+        // owner row: the first row whose inclusive prefix exceeds the task
+        int lo = 0, hi = rows - 1;
+#pragma unroll
+        for (int it = 0; it < 10; it++) {  // 2^10 = kMaxBandRows
+            if (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (s_pref[mid] > task) hi = mid;
+                else lo = mid + 1;
+            }
+        }
+        const short2 b = s_band[lo];
+        const int x = (int)b.x + task - (s_pref[lo] - ((int)b.y - (int)b.x + 1));
+        step(task < total, x, lo);
+    }
+}
+
 // Sweep the tiles of one huge queued Gaussian with the whole CTA; on_step(v,
 // x, y) is called by every lane of a warp together, v = the tile's exact test.
 template <typename F>
 __device__ __forceinline__ void sweep_cta(const MassiveEntry& me, const PreprocessParams& a, short2* s_band,
-                                          unsigned lane, int warp, F&& on_step)
+                                          int* s_pref, int* s_wsum, unsigned lane, int warp, F&& on_step)
 {
     const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
     const float pw = me.ctr_power_depth.z;
@@ -777,16 +834,10 @@ __device__ __forceinline__ void sweep_cta(const MassiveEntry& me, const Preproce
             s_band[r] = make_short2((short)clo, (short)chi);
         }
         __syncthreads();
-        for (int r = warp; r < y_hi - y_lo; r += kWarps) {
-            const short2 band = s_band[r];
-            const int y = y_lo + r;
-            for (int x0 = band.x; x0 <= band.y; x0 += 32) {
-                const int x = x0 + (int)lane;
-                const bool v = x <= band.y && tile_hit(x, y, a.bx, a.by, c, q, pw);
-                on_step(v, x, y);
-            }
-        }
-        __syncthreads();  // s_band and on_step's shared counters are reused by the next entry
+        sweep_flat_cta(y_hi - y_lo, s_band, s_pref, s_wsum, lane, warp, [&](bool valid, int x, int r) {
+            on_step(valid && tile_hit(x, y_lo + r, a.bx, a.by, c, q, pw), x, y_lo + r);
+        });
+        __syncthreads();  // s_band, s_pref and on_step's shared counters are reused by the next entry
         return;
     }
     // Otherwise the CTA sweeps the rectangle in windows of (cols x rows)
@@ -899,7 +950,7 @@ __device__ __forceinline__ bool band_quads(const Band& e, int qy, int by, int bx
 // row's band, so its quad lies in the quad row's band.
 template <typename F>
 __device__ __forceinline__ void sweep_cta_quad(const MassiveEntry& me, const PreprocessParams& a, short2* s_band,
-                                               unsigned lane, int warp, F&& on_step)
+                                               int* s_pref, int* s_wsum, unsigned lane, int warp, F&& on_step)
 {
     const float2 c = {me.ctr_power_depth.x, me.ctr_power_depth.y};
     const float pw = me.ctr_power_depth.z;
@@ -918,15 +969,10 @@ __device__ __forceinline__ void sweep_cta_quad(const MassiveEntry& me, const Pre
             s_band[r] = make_short2((short)lo, (short)hi);
         }
         __syncthreads();
-        for (int r = warp; r < qy_hi - qy_lo; r += kWarps) {
-            const short2 band = s_band[r];
-            const int qy = qy_lo + r;
-            for (int x0 = band.x; x0 <= band.y; x0 += 32) {
-                const int qx = x0 + (int)lane;
-                const uint32_t m = qx <= band.y ? quad_mask(qx, qy, rmin, rmax, a.bx, a.by, c, q, pw) : 0u;
-                on_step(m != 0u, qx, qy, m);
-            }
-        }
+        sweep_flat_cta(qy_hi - qy_lo, s_band, s_pref, s_wsum, lane, warp, [&](bool valid, int qx, int r) {
+            const uint32_t m = valid ? quad_mask(qx, qy_lo + r, rmin, rmax, a.bx, a.by, c, q, pw) : 0u;
+            on_step(m != 0u, qx, qy_lo + r, m);
+        });
         __syncthreads();
         return;
     }
@@ -1044,6 +1090,8 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
     __shared__ uint32_t s_pos;
     __shared__ uint32_t s_wcnt[kWarps];
     __shared__ short2 s_band[kMaxBandRows];
+    __shared__ int s_pref[kMaxBandRows];
+    __shared__ int s_wsum[kWarps];
     const unsigned lane = threadIdx.x & 31u;
     const int warp = threadIdx.x >> 5;
     Stage st{s_keys[MODE == kMassiveEmit64 ? warp : 0], s_vals[MODE == kMassiveEmit64 ? warp : 0], 0};
@@ -1069,23 +1117,23 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
         const PreprocessParams& av = VIEWS ? a.views[(uint32_t)me.rect.x >> 16] : a;
         if (MODE == kMassiveEmit64 && QUAD) {
             const int qgx = quad_cols(av.gx);
-            sweep_cta_quad(me, av, s_band, lane, warp, [&](bool v, int qx, int qy, uint32_t m) {
+            sweep_cta_quad(me, av, s_band, s_pref, s_wsum, lane, warp, [&](bool v, int qx, int qy, uint32_t m) {
                 uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + qy * qgx + qx) << 32) | db;
                 stage_emit(st, out, v, key, gid | (m << kQuadShift), lane);
             });
         } else if (MODE == kMassiveEmit64) {
-            sweep_cta(me, av, s_band, lane, warp, [&](bool v, int x, int y) {
+            sweep_cta(me, av, s_band, s_pref, s_wsum, lane, warp, [&](bool v, int x, int y) {
                 uint64_t key = ((uint64_t)(uint32_t)(av.tile_base + y * av.gx + x) << 32) | db;
                 stage_emit(st, out, v, key, gid, lane);
             });
         } else if (MODE == kMassiveCount) {
             uint32_t cnt = 0;
             if (QUAD)
-                sweep_cta_quad(me, a, s_band, lane, warp, [&](bool v, int, int, uint32_t) {
+                sweep_cta_quad(me, a, s_band, s_pref, s_wsum, lane, warp, [&](bool v, int, int, uint32_t) {
                     cnt += __popc(__ballot_sync(GSR_FULL_MASK, v));
                 });
             else
-                sweep_cta(me, a, s_band, lane, warp, [&](bool v, int, int) {
+                sweep_cta(me, a, s_band, s_pref, s_wsum, lane, warp, [&](bool v, int, int) {
                     cnt += __popc(__ballot_sync(GSR_FULL_MASK, v));
                 });
             if (lane == 0) s_wcnt[warp] = cnt;
@@ -1115,11 +1163,11 @@ __global__ __launch_bounds__(kThreads) void k_emit_massive(const __grid_constant
             };
             if (QUAD) {
                 const int qgx = quad_cols(a.gx);
-                sweep_cta_quad(me, a, s_band, lane, warp, [&](bool v, int qx, int qy, uint32_t m) {
+                sweep_cta_quad(me, a, s_band, s_pref, s_wsum, lane, warp, [&](bool v, int qx, int qy, uint32_t m) {
                     put(v, (uint32_t)(qy * qgx + qx), gid | (m << kQuadShift));
                 });
             } else {
-                sweep_cta(me, a, s_band, lane, warp,
+                sweep_cta(me, a, s_band, s_pref, s_wsum, lane, warp,
                           [&](bool v, int x, int y) { put(v, (uint32_t)(y * a.gx + x), gid); });
             }
             // sweep_cta ended on a barrier, so s_pos is final; every thread
