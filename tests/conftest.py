@@ -10,7 +10,16 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
-    config.addinivalue_line("markers", "slow: long-running case")
+    config.addinivalue_line("markers", "slow: long-running case (run with GSR_SLOW=1)")
+
+
+def pytest_collection_modifyitems(config, items):
+    if os.environ.get("GSR_SLOW") == "1":
+        return
+    skip = pytest.mark.skip(reason="slow case: set GSR_SLOW=1 to run it")
+    for item in items:
+        if "slow" in item.keywords:
+            item.add_marker(skip)
 
 
 @pytest.fixture(scope="session")
