@@ -89,3 +89,27 @@ def test_batch_rejects_bad_layouts(cuda_device):
     with pytest.raises(GsrError):
         b.render(scs, views[:2])  # more Gaussians / tiles than the batcher holds
     b.close()
+
+
+def test_new_batcher_first_batch_on_a_nonblocking_stream(cuda_device):
+    """A batcher zero-fills its buffer block when it is created.  A batch
+    launched at once on a fresh non-blocking stream (which does not wait for
+    the legacy default stream the fill runs on) must find the fill finished:
+    creation waits for it.  Each round builds a large block (2^26 keys, a fill
+    of a few milliseconds) and renders on a new stream straight away."""
+    scs = _scenes(cuda_device)
+    bg = torch.tensor([0.0, 0.0, 0.0])
+    views = _cams(0.0)[:3]
+    ref, total = _single(scs, views, bg)
+    torch.cuda.synchronize()
+    for _ in range(3):
+        b = Batcher(4, 1 << 26, sum(s.num_vertex for s in scs), 1 << 16, cuda_device)
+        stream = torch.cuda.Stream(cuda_device)
+        vs = [View(si, cam, bg) for si, cam in views]
+        with torch.cuda.stream(stream):
+            b.render(scs, vs, variant=R.RENDER_PERSISTENT_FUSED, half=True, use_graph=False, stream=stream)
+        assert b.finish(stream) == total
+        for v, r in zip(vs, ref):
+            s = image_stats(v.out.cpu().numpy(), r.cpu().numpy())
+            assert s["max_abs"] <= 2 and s["psnr"] >= 50.0, s
+        b.close()
