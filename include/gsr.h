@@ -346,6 +346,69 @@ const uint32_t* gsr_batcher_status(const gsr_batcher* b);
  * it.  They change which scheme tests the tiles, never the keys. */
 gsr_status gsr_batcher_set_thresholds(gsr_batcher* b, int massive_area, int huge_area);
 
+/* ---- differentiable render -------------------------------------------------- */
+/* No counterpart in the reference, which renders only.  The forward takes raw
+ * parameters (means [P,3], log-scales [P,3], w-first quaternions [P,4],
+ * opacity logits [P], SH [P,48] f32), runs the scene transform, preprocess,
+ * sort and tile ranges at 16x16 tiles, and renders a float image [H,W,3]
+ * together with what the backward replays: each pixel's final transmittance
+ * T_final [H,W] and each tile's number of blended Gaussians n_tile [tiles].
+ * The sorted values, ranges, features and those two buffers must be kept for
+ * the backward, which takes dL/dimage and writes (accumulate = 0) or adds
+ * (accumulate != 0) the gradients of every raw parameter; grad_xy [P,2],
+ * grad_con [P,4] and grad_rgb [P,3] are its scratch.  Read the key count and
+ * status with gsr_read_status after the forward (GSR_OVERFLOW: grow
+ * key_capacity and run it again). */
+gsr_status gsr_train_forward(int P, const float* means, const float* log_scales, const float* quats,
+                             const float* logits, const float* shs, int width, int height, const float* cam_pos,
+                             const float* cam_rot, float focal_x, float focal_y, float z_far, float z_near,
+                             const float* bg_color, float* opacity, float* cov3d, int32_t* curr_offset,
+                             void* workspace, size_t workspace_bytes, uint64_t* keys_unsorted,
+                             uint32_t* values_unsorted, uint64_t* keys_sorted, uint32_t* values_sorted,
+                             int64_t key_capacity, float* points_xy, float* rgb_depth, float* conic_opacity,
+                             int32_t* ranges, int32_t* n_tile, float* T_final, float* image, gsr_stream_t stream);
+gsr_status gsr_train_backward(int P, const float* means, const float* log_scales, const float* quats,
+                              const float* logits, const float* shs, int width, int height, const float* cam_pos,
+                              const float* cam_rot, float focal_x, float focal_y, float z_far, float z_near,
+                              const float* bg_color, const int32_t* curr_offset, int64_t key_capacity,
+                              const uint32_t* values_sorted, const int32_t* ranges, const int32_t* n_tile,
+                              const float* T_final, const float* points_xy, const float* rgb_depth,
+                              const float* conic_opacity, const float* grad_image, float* grad_xy, float* grad_con,
+                              float* grad_rgb, float* g_means, float* g_log_scales, float* g_quats, float* g_logits,
+                              float* g_shs, int accumulate, gsr_stream_t stream);
+/* The same over n_views cameras of one scene, all width x height, in one
+ * pass: one preprocess launch over every view, one sort over all keys (tile
+ * ids view * tiles + tile, values view * P + Gaussian), one tile-range pass,
+ * one render and one render backward over every view's tiles, and one
+ * preprocess adjoint per 16 views that sums the views' gradients per
+ * Gaussian.  Cameras are host arrays: cam_pos [n_views,3], cam_rot
+ * [n_views,9] and cam_intr [n_views,4] = (focal_x, focal_y, z_far, z_near).
+ * Per-view buffers follow one another: features and their gradients
+ * [n_views*P, ...], ranges and n_tile [n_views*tiles], T_final
+ * [n_views,H,W], image and grad_image [n_views,H,W,3].  view_scratch is
+ * device memory of gsr_train_views_scratch_bytes(n_views) for the views'
+ * parameter blocks; it must stay untouched until the forward has run. */
+size_t gsr_train_views_scratch_bytes(int n_views);
+gsr_status gsr_train_forward_views(int P, const float* means, const float* log_scales, const float* quats,
+                                   const float* logits, const float* shs, int n_views, int width, int height,
+                                   const float* cam_pos, const float* cam_rot, const float* cam_intr,
+                                   const float* bg_color, float* opacity, float* cov3d, void* view_scratch,
+                                   size_t view_scratch_bytes, int32_t* curr_offset, void* workspace,
+                                   size_t workspace_bytes, uint64_t* keys_unsorted, uint32_t* values_unsorted,
+                                   uint64_t* keys_sorted, uint32_t* values_sorted, int64_t key_capacity,
+                                   float* points_xy, float* rgb_depth, float* conic_opacity, int32_t* ranges,
+                                   int32_t* n_tile, float* T_final, float* image, gsr_stream_t stream);
+gsr_status gsr_train_backward_views(int P, const float* means, const float* log_scales, const float* quats,
+                                    const float* logits, const float* shs, int n_views, int width, int height,
+                                    const float* cam_pos, const float* cam_rot, const float* cam_intr,
+                                    const float* bg_color, const int32_t* curr_offset, int64_t key_capacity,
+                                    const uint32_t* values_sorted, const int32_t* ranges, const int32_t* n_tile,
+                                    const float* T_final, const float* points_xy, const float* rgb_depth,
+                                    const float* conic_opacity, const float* grad_image, float* grad_xy,
+                                    float* grad_con, float* grad_rgb, float* g_means, float* g_log_scales,
+                                    float* g_quats, float* g_logits, float* g_shs, int accumulate,
+                                    gsr_stream_t stream);
+
 /* ---- stage timing ------------------------------------------------------- */
 /* Profiling hook with no counterpart in the reference.  After
  * gsr_profile_begin(frames), each of the next `frames` gsr_forward calls

@@ -82,6 +82,66 @@ static bool valid_tile_shape(int bx, int by)
     return (bx == 16 && by == 16) || (bx == 32 && by == 16) || (bx == 24 && by == 16) || (bx == 32 && by == 32);
 }
 
+gsr_status preprocess_params(PreprocessParams& p, int P, const float* pos, const void* shs,
+                             const float* opacity, const float* cov3d, int width, int height, int block_x,
+                             int block_y, const float* cam_pos, const float* cam_rot, float fx, float fy,
+                             float zfar, float znear, float* points_xy, float* rgb_depth,
+                             float* conic_opacity, uint64_t* keys, uint32_t* values, int64_t cap,
+                             int32_t* curr_offset, void* workspace, size_t workspace_bytes)
+{
+    if (P < 0 || width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0 || !cam_pos || !cam_rot || !curr_offset)
+        return GSR_INVALID_ARG;
+    if (P > 0 && (!pos || !shs || !opacity || !cov3d || !points_xy || !rgb_depth || !conic_opacity))
+        return GSR_INVALID_ARG;
+    if (cap > 0 && (!keys || !values)) return GSR_INVALID_ARG;
+    p.df = DepthFirstRecords{nullptr, nullptr, nullptr, nullptr, 0};
+    p.gid_base = 0;
+    p.tile_base = 0;
+    p.views = nullptr;
+    p.n_views = 0;
+    p.massive_area = kDefaultMassiveArea;
+    p.huge_area = kDefaultHugeArea;
+    p.P = P;
+    p.pos = pos;
+    p.shs = shs;
+    p.opacity = opacity;
+    p.cov3d = cov3d;
+    p.W = width;
+    p.H = height;
+    p.bx = block_x;
+    p.by = block_y;
+    p.gx = div_up(width, block_x);
+    p.gy = div_up(height, block_y);
+    camera_matrices(width, height, cam_pos, cam_rot, fx, fy, zfar, znear, p.view, p.proj);
+    p.campos[0] = cam_pos[0];
+    p.campos[1] = cam_pos[1];
+    p.campos[2] = cam_pos[2];
+    p.tanx = width / (2.0f * fx);
+    p.tany = height / (2.0f * fy);
+    p.fx = fx;
+    p.fy = fy;
+    p.points_xy = reinterpret_cast<float2*>(points_xy);
+    p.rgb_depth = reinterpret_cast<float4*>(rgb_depth);
+    p.conic_opacity = reinterpret_cast<float4*>(conic_opacity);
+    p.keys = keys;
+    p.vals = values;
+    p.cap = cap;
+    p.counter = curr_offset;
+    p.mq.capacity = p.mq.huge_capacity = 0;
+    p.mq.entries = nullptr;
+    p.mq.count = p.mq.head = p.mq.depth_hi = nullptr;
+    if (workspace && workspace_bytes >= kSmallWorkspaceBytes) {
+        WorkspaceHeader* h = reinterpret_cast<WorkspaceHeader*>(workspace);
+        p.mq.entries = reinterpret_cast<MassiveEntry*>(reinterpret_cast<char*>(workspace) + kHeaderBytes);
+        p.mq.capacity = kMassiveQueueEntries;
+        p.mq.huge_capacity = kMassiveHugeEntries;
+        p.mq.count = h->mq_count;
+        p.mq.head = &h->mq_head[0][0];
+        p.mq.depth_hi = &h->depth_hi;
+    }
+    return GSR_OK;
+}
+
 }  // namespace gsr
 
 using namespace gsr;
@@ -200,66 +260,6 @@ gsr_status gsr_scene_prepare(int P, const float* log_scales, const float* quats,
 {
     if (P < 0 || (P > 0 && (!log_scales || !quats || !opacity_logits || !opacity || !cov3d))) return GSR_INVALID_ARG;
     return from_cuda(launch_scene_prepare(P, log_scales, quats, opacity_logits, opacity, cov3d, (cudaStream_t)stream));
-}
-
-static gsr_status preprocess_params(PreprocessParams& p, int P, const float* pos, const void* shs,
-                                    const float* opacity, const float* cov3d, int width, int height, int block_x,
-                                    int block_y, const float* cam_pos, const float* cam_rot, float fx, float fy,
-                                    float zfar, float znear, float* points_xy, float* rgb_depth,
-                                    float* conic_opacity, uint64_t* keys, uint32_t* values, int64_t cap,
-                                    int32_t* curr_offset, void* workspace, size_t workspace_bytes)
-{
-    if (P < 0 || width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0 || !cam_pos || !cam_rot || !curr_offset)
-        return GSR_INVALID_ARG;
-    if (P > 0 && (!pos || !shs || !opacity || !cov3d || !points_xy || !rgb_depth || !conic_opacity))
-        return GSR_INVALID_ARG;
-    if (cap > 0 && (!keys || !values)) return GSR_INVALID_ARG;
-    p.df = DepthFirstRecords{nullptr, nullptr, nullptr, nullptr, 0};
-    p.gid_base = 0;
-    p.tile_base = 0;
-    p.views = nullptr;
-    p.n_views = 0;
-    p.massive_area = kDefaultMassiveArea;
-    p.huge_area = kDefaultHugeArea;
-    p.P = P;
-    p.pos = pos;
-    p.shs = shs;
-    p.opacity = opacity;
-    p.cov3d = cov3d;
-    p.W = width;
-    p.H = height;
-    p.bx = block_x;
-    p.by = block_y;
-    p.gx = div_up(width, block_x);
-    p.gy = div_up(height, block_y);
-    camera_matrices(width, height, cam_pos, cam_rot, fx, fy, zfar, znear, p.view, p.proj);
-    p.campos[0] = cam_pos[0];
-    p.campos[1] = cam_pos[1];
-    p.campos[2] = cam_pos[2];
-    p.tanx = width / (2.0f * fx);
-    p.tany = height / (2.0f * fy);
-    p.fx = fx;
-    p.fy = fy;
-    p.points_xy = reinterpret_cast<float2*>(points_xy);
-    p.rgb_depth = reinterpret_cast<float4*>(rgb_depth);
-    p.conic_opacity = reinterpret_cast<float4*>(conic_opacity);
-    p.keys = keys;
-    p.vals = values;
-    p.cap = cap;
-    p.counter = curr_offset;
-    p.mq.capacity = p.mq.huge_capacity = 0;
-    p.mq.entries = nullptr;
-    p.mq.count = p.mq.head = p.mq.depth_hi = nullptr;
-    if (workspace && workspace_bytes >= kSmallWorkspaceBytes) {
-        WorkspaceHeader* h = reinterpret_cast<WorkspaceHeader*>(workspace);
-        p.mq.entries = reinterpret_cast<MassiveEntry*>(reinterpret_cast<char*>(workspace) + kHeaderBytes);
-        p.mq.capacity = kMassiveQueueEntries;
-        p.mq.huge_capacity = kMassiveHugeEntries;
-        p.mq.count = h->mq_count;
-        p.mq.head = &h->mq_head[0][0];
-        p.mq.depth_hi = &h->depth_hi;
-    }
-    return GSR_OK;
 }
 
 static gsr_status preprocess_impl(int P, const float* pos, const void* shs, int shs_half, const float* opacity,

@@ -97,6 +97,14 @@ constexpr int kDefaultHugeArea = 2048;
 void camera_matrices(int W, int H, const float* pos, const float* rot, float fx, float fy, float zfar, float znear,
                      float* view, float* proj);
 cudaError_t launch_preprocess(const PreprocessParams& p, bool half_sh, cudaStream_t stream);
+// Parameter block of one single-view preprocess (what gsr_preprocess fills),
+// with the large-Gaussian queue in the workspace when it is large enough.
+gsr_status preprocess_params(PreprocessParams& p, int P, const float* pos, const void* shs, const float* opacity,
+                             const float* cov3d, int width, int height, int block_x, int block_y,
+                             const float* cam_pos, const float* cam_rot, float fx, float fy, float zfar, float znear,
+                             float* points_xy, float* rgb_depth, float* conic_opacity, uint64_t* keys,
+                             uint32_t* values, int64_t cap, int32_t* curr_offset, void* workspace,
+                             size_t workspace_bytes);
 // One preprocess (+ large-Gaussian emission) over n_views views whose
 // parameter blocks are in device memory at base.views (shared fields --
 // queue, keys, counter -- are the same in every block and in `base`).
@@ -253,9 +261,14 @@ cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream);
 // Differentiable render (16x16 tiles, lite exit cadence 8): the forward
 // writes `image` (float [H,W,3]), `T_final` ([H,W]) and `n_tile` ([tiles]);
 // the backward reads them with `grad_image` and accumulates the per-Gaussian
-// gradients of xy [P,2], conic/opacity [P,4] and colour [P,3].
+// gradients of xy [P,2], conic/opacity [P,4] and colour [P,3].  With
+// n_views > 1 the views (all W x H) follow one another: tile t of view v is
+// global tile v * tiles + t in `ranges` and `n_tile`, and the per-pixel
+// buffers are [n_views, H, W(, 3)]; P then counts the feature rows of all
+// views.
 struct TrainRenderArgs {
     int W, H, P;
+    int n_views;  // 0 or 1: one view
     const int32_t* d_num;
     long long cap;
     const uint32_t* vals;

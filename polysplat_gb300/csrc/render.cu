@@ -589,11 +589,14 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_train(const TrainRe
     const unsigned lane = threadIdx.x & 31u;
     const int warp = threadIdx.x >> 5;
     TrainBatch& B = sb[warp];
+    // tile: global over the views; lt: within its view
     const int gx = (a.W + 15) / 16, tiles = gx * ((a.H + 15) / 16);
     const int tile = blockIdx.x * kTrainWarps + warp;
-    if (tile >= tiles) return;
+    if (tile >= tiles * max(a.n_views, 1)) return;
+    const int view = tile / tiles, lt = tile - view * tiles;
+    const size_t pix0 = (size_t)view * a.W * a.H;
     const int n = (int)max(0LL, min((long long)*a.d_num, a.cap));
-    const int ox = (tile % gx) * 16, oy = (tile / gx) * 16;
+    const int ox = (lt % gx) * 16, oy = (lt / gx) * 16;
     const int cb = (int)(lane & 7u) * 2, rb = (int)(lane >> 3) * 4;
     const int2 rg = __ldg(a.ranges + tile);
     const int start = min(max(rg.x, 0), n), end = min(max(rg.y, start), n);
@@ -647,7 +650,7 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_train(const TrainRe
         for (int j = 0; j < 2; j++) {
             const int px = ox + cb + j, py = oy + rb + i;
             if (px >= a.W || py >= a.H) continue;
-            const size_t o = (size_t)py * a.W + px;
+            const size_t o = pix0 + (size_t)py * a.W + px;
             const float t = T[i][j], tt = t < 0.0001f ? 0.0f : t;
             a.T_final[o] = t;
             a.image[3 * o + 0] = C[i][j][0] + tt * a.bg[0];
@@ -681,9 +684,11 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_backward(const Trai
     TrainBatch& B = sb[warp];
     const int gx = (a.W + 15) / 16, tiles = gx * ((a.H + 15) / 16);
     const int tile = blockIdx.x * kTrainWarps + warp;
-    if (tile >= tiles) return;
+    if (tile >= tiles * max(a.n_views, 1)) return;
+    const int view = tile / tiles, lt = tile - view * tiles;
+    const size_t pix0 = (size_t)view * a.W * a.H;
     const int n = (int)max(0LL, min((long long)*a.d_num, a.cap));
-    const int ox = (tile % gx) * 16, oy = (tile / gx) * 16;
+    const int ox = (lt % gx) * 16, oy = (lt / gx) * 16;
     const int cb = (int)(lane & 7u) * 2, rb = (int)(lane >> 3) * 4;
     const int2 rg = __ldg(a.ranges + tile);
     const int start = min(max(rg.x, 0), n);
@@ -695,7 +700,7 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_backward(const Trai
         for (int j = 0; j < 2; j++) {
             const int px = ox + cb + j, py = oy + rb + i;
             const bool in = px < a.W && py < a.H;
-            const size_t o = in ? (size_t)py * a.W + px : 0;
+            const size_t o = in ? pix0 + (size_t)py * a.W + px : 0;
             const float t = in ? __ldg(a.T_final + o) : 1.0f;
             T[i][j] = t;
 #pragma unroll
@@ -787,9 +792,10 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_backward(const Trai
 
 cudaError_t launch_render_train(const TrainRenderArgs& a, bool backward, cudaStream_t stream)
 {
-    const int tiles = ((a.W + 15) / 16) * ((a.H + 15) / 16);
+    const long long tiles = (long long)((a.W + 15) / 16) * ((a.H + 15) / 16) * max(a.n_views, 1);
     if (tiles <= 0) return cudaSuccess;
-    const int grid = div_up(tiles, kTrainWarps);
+    if (tiles > INT32_MAX - kTrainWarps) return cudaErrorInvalidValue;
+    const int grid = div_up((int)tiles, kTrainWarps);
     if (backward) k_render_backward<<<grid, kTrainWarps * 32, 0, stream>>>(a);
     else k_render_train<<<grid, kTrainWarps * 32, 0, stream>>>(a);
     return cudaGetLastError();

@@ -10,6 +10,13 @@ backward walks every tile's list in reverse (``k_render_backward``) and
 applies the per-Gaussian preprocess adjoint (``csrc/adjoint.h``) to reach the
 raw parameters: means, log-scales, w-first quaternions, opacity logits and
 SH coefficients.
+
+``render_views`` renders several cameras of one size in one pass
+(``gsr_train_forward_views`` / ``gsr_train_backward_views``): one preprocess
+launch over every view, one sort of all views' keys, one render and one
+render backward over every view's tiles, and one adjoint launch per 16 views
+that sums the views' gradients per Gaussian, so the parameters are read and
+their gradients written once per pass instead of once per camera.
 """
 from __future__ import annotations
 
@@ -109,7 +116,97 @@ def render(means: torch.Tensor, log_scales: torch.Tensor, quats: torch.Tensor, l
     return out
 
 
+def _views_cam_args(cams: Sequence[Camera]):
+    pos = [float(v) for c in cams for v in c.position.reshape(-1).tolist()]
+    rot = [float(v) for c in cams for v in c.rotation.reshape(-1).tolist()]
+    intr = [float(v) for c in cams for v in (c.focal_x, c.focal_y, c.zFar, c.zNear)]
+    return (ctypes.c_float * len(pos))(*pos), (ctypes.c_float * len(rot))(*rot), (ctypes.c_float * len(intr))(*intr)
+
+
+class _RenderViewsFn(torch.autograd.Function):
+    """All views in one pass (gsr_train_forward_views / gsr_train_backward_views)."""
+
+    @staticmethod
+    def forward(ctx, means, log_scales, quats, logits, shs, cams, bg, key_capacity):
+        dev = means.device
+        P, V = means.shape[0], len(cams)
+        W, H = cams[0].width, cams[0].height
+        tiles = ((W + 15) // 16) * ((H + 15) // 16)
+        pos, rot, intr = _views_cam_args(cams)
+        bgc = (ctypes.c_float * 3)(*[float(v) for v in bg])
+        params = [t.detach().contiguous().float() for t in (means, log_scales, quats, logits, shs.reshape(P, 48))]
+        stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        scratch = torch.empty(lib().gsr_train_views_scratch_bytes(V), dtype=torch.int8, device=dev)
+        cap = int(key_capacity)
+        while True:
+            b = dict(
+                opacity=torch.empty(P, device=dev), cov3d=torch.empty((P, 6), device=dev),
+                count=torch.zeros(1, dtype=torch.int32, device=dev),
+                ws=torch.empty(get_sort_buffer_size(cap), dtype=torch.int8, device=dev),
+                ku=torch.empty(cap, dtype=torch.int64, device=dev), vu=torch.empty(cap, dtype=torch.int32, device=dev),
+                ks=torch.empty(cap, dtype=torch.int64, device=dev), vs=torch.empty(cap, dtype=torch.int32, device=dev),
+                xy=torch.empty((V * P, 2), device=dev), rgbd=torch.empty((V * P, 4), device=dev),
+                con=torch.empty((V * P, 4), device=dev), ranges=torch.empty((V * tiles, 2), dtype=torch.int32, device=dev),
+                n_tile=torch.empty(V * tiles, dtype=torch.int32, device=dev), T=torch.empty((V, H, W), device=dev),
+                image=torch.empty((V, H, W, 3), device=dev))
+            check(lib().gsr_train_forward_views(
+                P, *[_p(t) for t in params], V, W, H, pos, rot, intr, bgc, _p(b["opacity"]), _p(b["cov3d"]),
+                _p(scratch), scratch.numel(), _p(b["count"]), _p(b["ws"]), b["ws"].numel(), _p(b["ku"]), _p(b["vu"]),
+                _p(b["ks"]), _p(b["vs"]), cap, _p(b["xy"]), _p(b["rgbd"]), _p(b["con"]), _p(b["ranges"]),
+                _p(b["n_tile"]), _p(b["T"]), _p(b["image"]), stream), "train_forward_views")
+            n = ctypes.c_int32(0)
+            st = lib().gsr_read_status(_p(b["ws"]), _p(b["count"]), cap, ctypes.byref(n), stream)
+            if st == R.GSR_OVERFLOW:
+                cap = max(2 * cap, int(n.value * 1.25))
+                if cap >= 1 << 30:
+                    raise R.GsrError(st, "train_forward_views: more keys than one sort takes", n.value)
+                continue
+            check(st, "train_forward_views", n.value)
+            break
+        for k in ("ku", "ks", "ws", "opacity", "cov3d"):
+            del b[k]
+        ctx.b, ctx.cams, ctx.bg, ctx.cap = b, list(cams), [float(v) for v in bg], cap
+        ctx.save_for_backward(*params)
+        ctx.num_rendered = n.value
+        return b["image"]
+
+    @staticmethod
+    def backward(ctx, grad_image):
+        means, log_scales, quats, logits, shs = ctx.saved_tensors
+        b, cams = ctx.b, ctx.cams
+        dev = means.device
+        P, V = means.shape[0], len(cams)
+        g = grad_image.contiguous().float()
+        pos, rot, intr = _views_cam_args(cams)
+        bgc = (ctypes.c_float * 3)(*ctx.bg)
+        gxy, gcon, grgb = (torch.empty((V * P, 2), device=dev), torch.empty((V * P, 4), device=dev),
+                           torch.empty((V * P, 3), device=dev))
+        outs = [torch.empty_like(t) for t in (means, log_scales, quats, logits, shs)]
+        stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        check(lib().gsr_train_backward_views(
+            P, _p(means), _p(log_scales), _p(quats), _p(logits), _p(shs), V, cams[0].width, cams[0].height, pos, rot,
+            intr, bgc, _p(b["count"]), ctx.cap, _p(b["vs"]), _p(b["ranges"]), _p(b["n_tile"]), _p(b["T"]),
+            _p(b["xy"]), _p(b["rgbd"]), _p(b["con"]), _p(g), _p(gxy), _p(gcon), _p(grgb), *[_p(t) for t in outs], 0,
+            stream), "train_backward_views")
+        ctx.b = None
+        gm, gls, gq, glg, gsh = outs
+        return gm, gls, gq, glg, gsh, None, None, None
+
+
 def render_views(means, log_scales, quats, logits, shs, cameras: Sequence[Camera], bg=(0.0, 0.0, 0.0),
                  key_capacity: int = 1 << 22):
-    """One differentiable image per camera (gradients sum over views)."""
-    return [render(means, log_scales, quats, logits, shs, c, bg, key_capacity) for c in cameras]
+    """One differentiable image per camera (gradients sum over views).
+
+    Cameras of one size go through one pass over all views: one preprocess
+    launch, one sort of every view's keys, one render and one render backward
+    over every view's tiles, and one adjoint that sums the views' gradients
+    per Gaussian (`key_capacity` is per view).  Cameras of different sizes
+    fall back to one pass per camera."""
+    cams = list(cameras)
+    if not cams:
+        return []
+    if len(cams) == 1 or any((c.width, c.height) != (cams[0].width, cams[0].height) for c in cams):
+        return [render(means, log_scales, quats, logits, shs, c, bg, key_capacity) for c in cams]
+    cap = min(int(key_capacity) * len(cams), (1 << 30) - 1)
+    out = _RenderViewsFn.apply(means, log_scales, quats, logits, shs.reshape(shs.shape[0], 48), cams, list(bg), cap)
+    return list(out.unbind(0))
