@@ -71,6 +71,10 @@ def parse():
                     help="serve_mix only: skip the plain arm and the autotuner, serve the stream with this "
                          "TuneConfig (JSON, e.g. the bench line's config.tuned) twice to warm up and once more "
                          "inside the NVTX range 'timed', device-only: for ncu launch lists")
+    ap.add_argument("--diff-profile", action="store_true",
+                    help="diff_1m_8cam only: after three warm-up steps of each path, run one step through "
+                         "render_views inside the NVTX start/end range 'timed_views' and one with a pass per "
+                         "camera inside 'timed_loop': for ncu launch lists")
     ap.add_argument("--pipeline", default="single", choices=["single", "depth_first"],
                     help="single-pass 64-bit key sort, or depth sort + 32-bit tile sort")
     return ap.parse_args()
@@ -923,6 +927,18 @@ def run_diff(args, dev, rank, world, dist):
         return loss
 
     K = max(3, min(args.steps, 30))
+    if args.diff_profile:
+        for multi, name in ((True, "timed_views"), (False, "timed_loop")):
+            for _ in range(3):
+                step(multi)
+            torch.cuda.synchronize()
+            # a start/end range, not push/pop: the backward launches from
+            # autograd's own thread
+            rid = torch.cuda.nvtx.range_start(name)
+            step(multi)
+            torch.cuda.synchronize()
+            torch.cuda.nvtx.range_end(rid)
+        return {"workload": "diff_1m_8cam (profiling run)", "ranges": ["timed_views", "timed_loop"]}
 
     def timed(multi, sampler=None):
         for _ in range(max(3, args.warmup)):

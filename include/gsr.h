@@ -383,9 +383,11 @@ gsr_status gsr_train_backward(int P, const float* means, const float* log_scales
  * preprocess adjoint per 16 views that sums the views' gradients per
  * Gaussian.  Cameras are host arrays: cam_pos [n_views,3], cam_rot
  * [n_views,9] and cam_intr [n_views,4] = (focal_x, focal_y, z_far, z_near).
- * Per-view buffers follow one another: features and their gradients
- * [n_views*P, ...], ranges and n_tile [n_views*tiles], T_final
- * [n_views,H,W], image and grad_image [n_views,H,W,3].  view_scratch is
+ * Per-view buffers follow one another: features [n_views*P, ...], ranges
+ * and n_tile [n_views*tiles], T_final [n_views,H,W], image and grad_image
+ * [n_views,H,W,3].  The backward's scratch grad_feat [n_views*P, 12]
+ * (16-byte aligned) holds one record per feature row: the gradients of
+ * conic/opacity (4), xy (2) and colour (3), and 3 unused.  view_scratch is
  * device memory of gsr_train_views_scratch_bytes(n_views) for the views'
  * parameter blocks; it must stay untouched until the forward has run. */
 size_t gsr_train_views_scratch_bytes(int n_views);
@@ -404,10 +406,9 @@ gsr_status gsr_train_backward_views(int P, const float* means, const float* log_
                                     const float* bg_color, const int32_t* curr_offset, int64_t key_capacity,
                                     const uint32_t* values_sorted, const int32_t* ranges, const int32_t* n_tile,
                                     const float* T_final, const float* points_xy, const float* rgb_depth,
-                                    const float* conic_opacity, const float* grad_image, float* grad_xy,
-                                    float* grad_con, float* grad_rgb, float* g_means, float* g_log_scales,
-                                    float* g_quats, float* g_logits, float* g_shs, int accumulate,
-                                    gsr_stream_t stream);
+                                    const float* conic_opacity, const float* grad_image, float* grad_feat,
+                                    float* g_means, float* g_log_scales, float* g_quats, float* g_logits,
+                                    float* g_shs, int accumulate, gsr_stream_t stream);
 
 /* ---- stage timing ------------------------------------------------------- */
 /* Profiling hook with no counterpart in the reference.  After

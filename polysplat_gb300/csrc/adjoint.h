@@ -205,8 +205,10 @@ GSR_HD void forward(const T m[3], const T ls[3], const T q[4], T logit, const T*
     }
 }
 
-// Gradients of the raw parameters from those of xy, con and rgb.
-template <typename T>
+// Gradients of the raw parameters from those of xy, con and rgb.  ADD_SH:
+// add the SH gradient to g_sh instead of writing it (a caller summing over
+// views needs no second 48-entry array).
+template <typename T, bool ADD_SH = false>
 GSR_HD void backward(const T m[3], const T* sh, const Cam<T>& cam, const Tape<T>& tp, const T g_xy[2], const T g_con[4],
                      const T g_rgb[3], T g_m[3], T g_ls[3], T g_q[4], T& g_logit, T* g_sh)
 {
@@ -306,7 +308,8 @@ GSR_HD void backward(const T m[3], const T* sh, const Cam<T>& cam, const Tape<T>
     for (int ch = 0; ch < 3; ch++) {
         const T g = tp.clamp_rgb[ch] ? (T)0 : g_rgb[ch];
         for (int k = 0; k < 16; k++) {
-            g_sh[3 * k + ch] = tp.B[k] * g;
+            if (ADD_SH) g_sh[3 * k + ch] += tp.B[k] * g;
+            else g_sh[3 * k + ch] = tp.B[k] * g;
             for (int d = 0; d < 3; d++) g_dir[d] += tp.dB[k][d] * sh[3 * k + ch] * g;
         }
     }

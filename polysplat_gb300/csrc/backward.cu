@@ -88,11 +88,10 @@ struct PreBackViewsArgs {
     const float* logits;
     const float* shs;  // [P,48] f32
     gsr_adj::Cam<float> cam[kAdjViews];
-    // per-view gradients of the screen-space features: view v's rows start
-    // at v * P (of the launch's first view)
-    const float* gxy;
-    const float* gcon;
-    const float* grgb;
+    // per-view gradient records of the screen-space features (conic and
+    // opacity, xy, colour; 12 floats): view v's rows start at v * P (of the
+    // launch's first view)
+    const float4* grec;
     float* g_means;
     float* g_log_scales;
     float* g_quats;
@@ -115,17 +114,10 @@ __global__ __launch_bounds__(128) void k_preprocess_backward_views(const __grid_
     bool loaded = false;
     for (int v = 0; v < a.n_views; v++) {
         const size_t r = (size_t)v * a.P + i;
-        float gxy[2] = {a.gxy[2 * r], a.gxy[2 * r + 1]};
-        float gcon[4], grgb[3];
-        bool any = gxy[0] != 0.f || gxy[1] != 0.f;
-        for (int k = 0; k < 4; k++) {
-            gcon[k] = a.gcon[4 * r + k];
-            any |= gcon[k] != 0.f;
-        }
-        for (int k = 0; k < 3; k++) {
-            grgb[k] = a.grgb[3 * r + k];
-            any |= grgb[k] != 0.f;
-        }
+        const float4 q0 = a.grec[3 * r], q1 = a.grec[3 * r + 1], q2 = a.grec[3 * r + 2];
+        float gcon[4] = {q0.x, q0.y, q0.z, q0.w}, gxy[2] = {q1.x, q1.y}, grgb[3] = {q1.z, q1.w, q2.x};
+        const bool any = gcon[0] != 0.f || gcon[1] != 0.f || gcon[2] != 0.f || gcon[3] != 0.f || gxy[0] != 0.f ||
+                         gxy[1] != 0.f || grgb[0] != 0.f || grgb[1] != 0.f || grgb[2] != 0.f;
         if (!any) continue;
         if (!loaded) {
             for (int k = 0; k < 3; k++) {
@@ -140,15 +132,14 @@ __global__ __launch_bounds__(128) void k_preprocess_backward_views(const __grid_
         gsr_adj::Fwd<float> f;
         gsr_adj::Tape<float> tp;
         gsr_adj::forward(m, ls, q, logit, sh, a.cam[v], f, tp);
-        float vm[3], vls[3], vq[4], vlogit, vsh[48];
-        gsr_adj::backward(m, sh, a.cam[v], tp, gxy, gcon, grgb, vm, vls, vq, vlogit, vsh);
+        float vm[3], vls[3], vq[4], vlogit;
+        gsr_adj::backward<float, true>(m, sh, a.cam[v], tp, gxy, gcon, grgb, vm, vls, vq, vlogit, gsh);
         for (int k = 0; k < 3; k++) {
             gm[k] += vm[k];
             gls[k] += vls[k];
         }
         for (int k = 0; k < 4; k++) gq[k] += vq[k];
         glogit += vlogit;
-        for (int k = 0; k < 48; k++) gsh[k] += vsh[k];
     }
     if (!loaded && a.accumulate) return;
     auto put = [&](float* dst, size_t off, float v) { dst[off] = a.accumulate ? dst[off] + v : v; };
@@ -360,6 +351,7 @@ gsr_status gsr_train_forward_views(int P, const float* means, const float* log_s
     } else {
         PreprocessParams base = hp[0];
         base.n_views = n_views;
+        base.interleave = 1;  // every view has the scene's P
         // a pageable source is staged before the call returns
         e = cudaMemcpyAsync(d_params, hp.data(), sizeof(PreprocessParams) * (size_t)n_views, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = launch_preprocess_views(base, n_views, n_views * div_up(P, 256), false, s);
@@ -406,15 +398,15 @@ gsr_status gsr_train_backward_views(int P, const float* means, const float* log_
                                     const float* bg_color, const int32_t* curr_offset, int64_t key_capacity,
                                     const uint32_t* values_sorted, const int32_t* ranges, const int32_t* n_tile,
                                     const float* T_final, const float* points_xy, const float* rgb_depth,
-                                    const float* conic_opacity, const float* grad_image, float* grad_xy,
-                                    float* grad_con, float* grad_rgb, float* g_means, float* g_log_scales,
-                                    float* g_quats, float* g_logits, float* g_shs, int accumulate,
-                                    gsr_stream_t stream)
+                                    const float* conic_opacity, const float* grad_image, float* grad_feat,
+                                    float* g_means, float* g_log_scales, float* g_quats, float* g_logits,
+                                    float* g_shs, int accumulate, gsr_stream_t stream)
 {
     cudaStream_t s = (cudaStream_t)stream;
     if (P < 0 || n_views <= 0 || width <= 0 || height <= 0 || !cam_pos || !cam_rot || !cam_intr || !bg_color ||
-        !curr_offset || !ranges || !n_tile || !T_final || !grad_image || !grad_xy || !grad_con || !grad_rgb)
+        !curr_offset || !ranges || !n_tile || !T_final || !grad_image || !grad_feat)
         return GSR_INVALID_ARG;
+    if ((reinterpret_cast<uintptr_t>(grad_feat) & 15u) != 0) return GSR_INVALID_ARG;  // 16-byte atomics
     const int tiles = div_up(width, 16) * div_up(height, 16);
     if ((long long)P * n_views >= (1LL << 31) || (long long)tiles * n_views >= (1LL << 30)) return GSR_INVALID_ARG;
     if (P == 0) return GSR_OK;
@@ -422,9 +414,7 @@ gsr_status gsr_train_backward_views(int P, const float* means, const float* log_
         !g_shs || !values_sorted || !points_xy || !rgb_depth || !conic_opacity)
         return GSR_INVALID_ARG;
     const size_t rows = (size_t)P * n_views;
-    cudaError_t e = cudaMemsetAsync(grad_xy, 0, sizeof(float) * 2 * rows, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(grad_con, 0, sizeof(float) * 4 * rows, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(grad_rgb, 0, sizeof(float) * 3 * rows, s);
+    cudaError_t e = cudaMemsetAsync(grad_feat, 0, sizeof(float) * 12 * rows, s);
     if (e != cudaSuccess) return GSR_CUDA_ERROR;
     TrainRenderArgs ra = {};
     ra.W = width;
@@ -442,9 +432,7 @@ gsr_status gsr_train_backward_views(int P, const float* means, const float* log_
     ra.T_final = const_cast<float*>(T_final);
     ra.n_tile = const_cast<int32_t*>(n_tile);
     ra.grad_image = grad_image;
-    ra.grad_xy = grad_xy;
-    ra.grad_con = grad_con;
-    ra.grad_rgb = grad_rgb;
+    ra.grad_rec = grad_feat;
     if ((e = launch_render_train(ra, true, s)) != cudaSuccess) return GSR_CUDA_ERROR;
     for (int v0 = 0; v0 < n_views; v0 += kAdjViews) {
         PreBackViewsArgs pa;
@@ -461,10 +449,7 @@ gsr_status gsr_train_backward_views(int P, const float* means, const float* log_
             pa.cam[k] = adj_camera(width, height, cam_pos + 3 * (size_t)v, cam_rot + 9 * (size_t)v, in[0], in[1],
                                    in[2], in[3]);
         }
-        const size_t r0 = (size_t)v0 * P;
-        pa.gxy = grad_xy + 2 * r0;
-        pa.gcon = grad_con + 4 * r0;
-        pa.grgb = grad_rgb + 3 * r0;
+        pa.grec = reinterpret_cast<const float4*>(grad_feat) + 3 * (size_t)v0 * P;
         pa.g_means = g_means;
         pa.g_log_scales = g_log_scales;
         pa.g_quats = g_quats;

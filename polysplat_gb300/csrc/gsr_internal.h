@@ -81,6 +81,11 @@ struct PreprocessParams {
     // row-major over ceil(gx / 2) columns) and the hit tiles as a 4-bit mask
     // in the value's top bits (see kQuadShift).
     int quad = 0;
+    // Batches whose views all have the same P (views of one scene): block b
+    // takes view b % n_views and block b / n_views of that view, so the
+    // views' blocks over one range of Gaussians run side by side and the
+    // range's parameters come from DRAM once and from L2 for the other views.
+    int interleave = 0;
 };
 // Quad keys: bit (x & 1) | (y & 1) << 1 of value >> kQuadShift is set when
 // the Gaussian hits tile (x, y) of the quad, by the same exact tile test the
@@ -284,6 +289,10 @@ struct TrainRenderArgs {
     float* grad_xy;
     float* grad_con;
     float* grad_rgb;
+    // when set, replaces the three arrays above: one 12-float record per
+    // feature row, conic/opacity (4), xy (2), colour (3) and 3 unused, added
+    // to with three 16-byte atomics
+    float* grad_rec;
 };
 cudaError_t launch_render_train(const TrainRenderArgs& a, bool backward, cudaStream_t stream);
 

@@ -350,7 +350,11 @@ __global__ __launch_bounds__(kThreads, VIEWS ? 6 : 5) void k_preprocess(const __
     // VIEWS: the views' blocks follow one another along the grid (parameter
     // blocks in device memory); a block past the last view has no work
     int vi = 0, lblock = (int)blockIdx.x;
-    if (VIEWS) {
+    if (VIEWS && a0.interleave) {
+        vi = (int)(blockIdx.x % (unsigned)a0.n_views);
+        lblock = (int)(blockIdx.x / (unsigned)a0.n_views);
+        if (lblock >= (a0.views[vi].P + kThreads - 1) / kThreads) return;
+    } else if (VIEWS) {
         vi = -1;
         for (int u = 0, start = 0; u < a0.n_views; u++) {
             const int nb = (a0.views[u].P + kThreads - 1) / kThreads;

@@ -666,6 +666,28 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
+// Sums of eight values over the warp in 9 shuffles instead of 40: at each of
+// the first three steps a lane keeps half of its partial sums and sends the
+// other half to its partner.  Lane l returns the total of
+// v[((l >> 4) & 1) * 4 + ((l >> 3) & 1) * 2 + ((l >> 2) & 1)], that is
+// v[l >> 2] for every lane l with l & 3 == 0.
+__device__ __forceinline__ float warp_sum8_spread(const float (&v)[8], unsigned lane)
+{
+    const bool b4 = (lane & 16u) != 0u, b3 = (lane & 8u) != 0u, b2 = (lane & 4u) != 0u;
+    float h[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        h[k] = (b4 ? v[k + 4] : v[k]) + __shfl_xor_sync(GSR_FULL_MASK, b4 ? v[k] : v[k + 4], 16);
+    float q[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+        q[k] = (b3 ? h[k + 2] : h[k]) + __shfl_xor_sync(GSR_FULL_MASK, b3 ? h[k] : h[k + 2], 8);
+    float t = (b2 ? q[1] : q[0]) + __shfl_xor_sync(GSR_FULL_MASK, b2 ? q[0] : q[1], 4);
+    t += __shfl_xor_sync(GSR_FULL_MASK, t, 2);
+    t += __shfl_xor_sync(GSR_FULL_MASK, t, 1);
+    return t;
+}
+
 // Reverse traversal of each tile's blended Gaussians.  With T_after the
 // transmittance behind Gaussian i and alpha_i recomputed bit for bit,
 // T_before = T_after / (1 - alpha_i) (1 - alpha is exact once alpha >= 1/2);
@@ -675,7 +697,8 @@ __device__ __forceinline__ float warp_sum(float v)
 //   dL/dc_i     = sum_px alpha_i T_before dL/dC
 //   dL/dalpha_i = T_before (c_i - R) . dL/dC,   d alpha/d power = alpha ln 2
 // and the power's derivatives give the conic/opacity and centre gradients.
-// The 9 per-Gaussian sums are reduced over the warp and added atomically.
+// The 9 per-Gaussian sums are reduced over the warp (eight of them spread
+// over the lanes, warp_sum8_spread) and added atomically by nine lanes.
 __global__ __launch_bounds__(kTrainWarps * 32) void k_render_backward(const TrainRenderArgs a)
 {
     __shared__ TrainBatch sb[kTrainWarps];
@@ -727,7 +750,11 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_backward(const Trai
             const float4 co = B.con[k];
             const float4 c4 = B.rgb[k];
             const float col[3] = {c4.x, c4.y, c4.z};
-            float gcon[4] = {0.f, 0.f, 0.f, 0.f}, gxy[2] = {0.f, 0.f}, gc[3] = {0.f, 0.f, 0.f};
+            float gc[3] = {0.f, 0.f, 0.f};
+            // dx depends on the column only and dy on the row only, so the
+            // conic and centre gradients need three sums over this lane's
+            // pixels of dp (per column, per row) and of dp * dx (per row)
+            float s_col[2] = {0.f, 0.f}, g_w = 0.f, g_yy = 0.f, g_xy = 0.f, sy = 0.f, sx = 0.f;
             // the forward's per-pixel power, term for term (shade<>, SHADER 0)
             float xs[2], xc[2], dxs[2];
 #pragma unroll
@@ -741,6 +768,7 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_backward(const Trai
             for (int i = 0; i < 4; i++) {
                 const float dy = xy.y - (float)(oy + rb + i);
                 const float ys = co.z * dy * dy;
+                float r = 0.f, q = 0.f;
 #pragma unroll
                 for (int j = 0; j < 2; j++) {
                     const float power = fmaf(xc[j], dy, co.w + xs[j] + ys);
@@ -751,38 +779,64 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_backward(const Trai
                     float dalpha = 0.0f;
 #pragma unroll
                     for (int ch = 0; ch < 3; ch++) {
-                        gc[ch] += w * G[i][j][ch];
-                        dalpha += (col[ch] - R[i][j][ch]) * G[i][j][ch];
-                        R[i][j][ch] = alpha * col[ch] + one_m * R[i][j][ch];
+                        const float d = col[ch] - R[i][j][ch];
+                        gc[ch] = fmaf(w, G[i][j][ch], gc[ch]);
+                        dalpha = fmaf(d, G[i][j][ch], dalpha);
+                        R[i][j][ch] = fmaf(alpha, d, R[i][j][ch]);  // alpha c + (1 - alpha) R
                     }
                     T[i][j] = Tb;
-                    const float dp = dalpha * Tb * alpha * LN2;
-                    const float dx = dxs[j];
-                    gcon[3] += dp;
-                    gcon[0] += dp * dx * dx;
-                    gcon[2] += dp * dy * dy;
-                    gcon[1] += dp * dx * dy;
-                    gxy[0] += dp * (2.0f * co.x * dx + co.y * dy);
-                    gxy[1] += dp * (2.0f * co.z * dy + co.y * dx);
+                    // d power of this pixel, without its factor ln 2 (applied to the totals)
+                    const float dp = dalpha * w;
+                    r += dp;
+                    q = fmaf(dp, dxs[j], q);
+                    s_col[j] += dp;
                 }
+                g_w += r;
+                g_yy = fmaf(dy * dy, r, g_yy);
+                g_xy = fmaf(dy, q, g_xy);
+                sy = fmaf(dy, r, sy);
+                sx += q;
             }
-#pragma unroll
-            for (int q = 0; q < 4; q++) gcon[q] = warp_sum(gcon[q]);
-#pragma unroll
-            for (int q = 0; q < 2; q++) gxy[q] = warp_sum(gxy[q]);
-#pragma unroll
-            for (int q = 0; q < 3; q++) gc[q] = warp_sum(gc[q]);
+            // d power / d (conic x, y, z, w) = (dx^2, dx dy, dy^2, 1);
+            // d power / d centre = (2 co.x dx + co.y dy, 2 co.z dy + co.y dx)
+            float v[8];
+            v[0] = LN2 * fmaf(dxs[0] * dxs[0], s_col[0], dxs[1] * dxs[1] * s_col[1]);
+            v[1] = LN2 * g_xy;
+            v[2] = LN2 * g_yy;
+            v[3] = LN2 * g_w;
+            v[4] = LN2 * fmaf(2.0f * co.x, sx, co.y * sy);
+            v[5] = LN2 * fmaf(2.0f * co.z, sy, co.y * sx);
+            v[6] = gc[0];
+            v[7] = gc[1];
+            const float t8 = warp_sum8_spread(v, lane);
+            const float t9 = warp_sum(gc[2]);
+            // lanes 0, 4, .., 28 hold the totals of v[lane / 4]; every lane the ninth
             const uint32_t gid = B.gid[k];
-            if (lane == 0 && gid != 0xFFFFFFFFu) {
-                atomicAdd(a.grad_con + 4 * (size_t)gid + 0, gcon[0]);
-                atomicAdd(a.grad_con + 4 * (size_t)gid + 1, gcon[1]);
-                atomicAdd(a.grad_con + 4 * (size_t)gid + 2, gcon[2]);
-                atomicAdd(a.grad_con + 4 * (size_t)gid + 3, gcon[3]);
-                atomicAdd(a.grad_xy + 2 * (size_t)gid + 0, gxy[0]);
-                atomicAdd(a.grad_xy + 2 * (size_t)gid + 1, gxy[1]);
-                atomicAdd(a.grad_rgb + 3 * (size_t)gid + 0, gc[0]);
-                atomicAdd(a.grad_rgb + 3 * (size_t)gid + 1, gc[1]);
-                atomicAdd(a.grad_rgb + 3 * (size_t)gid + 2, gc[2]);
+            if (a.grad_rec) {
+                // lane L < 3 adds slots 4L .. 4L + 3 of the Gaussian's record
+                float r4[4];
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const int slot = 4 * (int)(lane & 3u) + c;
+                    const float x = __shfl_sync(GSR_FULL_MASK, t8, slot < 8 ? 4 * slot : 0);
+                    r4[c] = slot < 8 ? x : (slot == 8 ? t9 : 0.0f);
+                }
+                if (lane < 3u && gid != 0xFFFFFFFFu)
+                    atomicAdd(reinterpret_cast<float4*>(a.grad_rec + 12 * (size_t)gid) + lane,
+                              make_float4(r4[0], r4[1], r4[2], r4[3]));
+            } else if (gid != 0xFFFFFFFFu) {
+                float* dst = nullptr;
+                float val = t8;
+                if ((lane & 3u) == 0u) {
+                    const int q8 = (int)(lane >> 2);
+                    dst = q8 < 4 ? a.grad_con + 4 * (size_t)gid + q8
+                        : q8 < 6 ? a.grad_xy + 2 * (size_t)gid + (q8 - 4)
+                                 : a.grad_rgb + 3 * (size_t)gid + (q8 - 6);
+                } else if (lane == 1u) {
+                    dst = a.grad_rgb + 3 * (size_t)gid + 2;
+                    val = t9;
+                }
+                if (dst) atomicAdd(dst, val);
             }
         }
     }

@@ -179,14 +179,13 @@ class _RenderViewsFn(torch.autograd.Function):
         g = grad_image.contiguous().float()
         pos, rot, intr = _views_cam_args(cams)
         bgc = (ctypes.c_float * 3)(*ctx.bg)
-        gxy, gcon, grgb = (torch.empty((V * P, 2), device=dev), torch.empty((V * P, 4), device=dev),
-                           torch.empty((V * P, 3), device=dev))
+        gfeat = torch.empty((V * P, 12), device=dev)
         outs = [torch.empty_like(t) for t in (means, log_scales, quats, logits, shs)]
         stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
         check(lib().gsr_train_backward_views(
             P, _p(means), _p(log_scales), _p(quats), _p(logits), _p(shs), V, cams[0].width, cams[0].height, pos, rot,
             intr, bgc, _p(b["count"]), ctx.cap, _p(b["vs"]), _p(b["ranges"]), _p(b["n_tile"]), _p(b["T"]),
-            _p(b["xy"]), _p(b["rgbd"]), _p(b["con"]), _p(g), _p(gxy), _p(gcon), _p(grgb), *[_p(t) for t in outs], 0,
+            _p(b["xy"]), _p(b["rgbd"]), _p(b["con"]), _p(g), _p(gfeat), *[_p(t) for t in outs], 0,
             stream), "train_backward_views")
         ctx.b = None
         gm, gls, gq, glg, gsh = outs
