@@ -699,7 +699,10 @@ __device__ __forceinline__ float warp_sum8_spread(const float (&v)[8], unsigned 
 // and the power's derivatives give the conic/opacity and centre gradients.
 // The 9 per-Gaussian sums are reduced over the warp (eight of them spread
 // over the lanes, warp_sum8_spread) and added atomically by nine lanes.
-__global__ __launch_bounds__(kTrainWarps * 32) void k_render_backward(const TrainRenderArgs a)
+// Five CTAs of 128 threads per SM (96 registers, a few bytes spilled): the
+// kernel is bound by instruction issue with few warps resident, and the
+// fifth CTA measured 1-2% faster per config-4 step than four at 120 registers.
+__global__ __launch_bounds__(kTrainWarps * 32, 5) void k_render_backward(const TrainRenderArgs a)
 {
     __shared__ TrainBatch sb[kTrainWarps];
     const unsigned lane = threadIdx.x & 31u;
