@@ -290,3 +290,42 @@ def test_render_views_of_mixed_sizes_runs_per_view(cuda_device):
     assert [tuple(i.shape) for i in imgs] == [(96, 160, 3), (96, 160, 3), (80, 128, 3)]
     d = (imgs[2] - ref).abs()
     assert float(d.max()) <= 2.0 / 255.0 and int((d > 1e-5).sum()) <= 1e-4 * d.numel()
+
+
+def test_training_view_entries_reject_bad_arguments(cuda_device):
+    """The multi-view entries check their arguments before any launch: no
+    views, a parameter scratch smaller than gsr_train_views_scratch_bytes, and
+    a gradient record buffer off a 16-byte boundary (the record atomics
+    are 16 bytes wide) return GSR_INVALID_ARG."""
+    import ctypes
+
+    from polysplat_gb300._lib import GSR_INVALID_ARG, lib
+
+    dev = cuda_device
+    L = lib()
+    assert L.gsr_train_views_scratch_bytes(0) == 0
+    assert L.gsr_train_views_scratch_bytes(8) >= 8 * 64
+    P, V, W, H = 16, 2, 32, 32
+    buf = torch.zeros(1 << 20, dtype=torch.float32, device=dev)
+    p = ctypes.c_void_p(buf.data_ptr())
+    pos = (ctypes.c_float * (3 * V))()
+    rot = (ctypes.c_float * (9 * V))()
+    intr = (ctypes.c_float * (4 * V))(*([100.0, 100.0, 100.0, 0.01] * V))
+    bg = (ctypes.c_float * 3)()
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    ws = L.gsr_workspace_size(1 << 10)
+
+    def fwd(n_views, scratch_bytes):
+        return L.gsr_train_forward_views(P, p, p, p, p, p, n_views, W, H, pos, rot, intr, bg, p, p, p,
+                                         scratch_bytes, p, p, ws, p, p, p, p, 1 << 10, p, p, p, p, p, p, p, stream)
+
+    assert fwd(0, 1 << 20) == GSR_INVALID_ARG
+    assert fwd(V, L.gsr_train_views_scratch_bytes(V) - 1) == GSR_INVALID_ARG
+
+    def bwd(grad_feat):
+        return L.gsr_train_backward_views(P, p, p, p, p, p, V, W, H, pos, rot, intr, bg, p, 1 << 10, p, p, p, p,
+                                          p, p, p, p, grad_feat, p, p, p, p, p, 0, stream)
+
+    assert bwd(ctypes.c_void_p(buf.data_ptr() + 4)) == GSR_INVALID_ARG
+    assert bwd(None) == GSR_INVALID_ARG
+    torch.cuda.synchronize()

@@ -122,3 +122,22 @@ def test_serve_mix_shape():
     t = [r.arrival_s for r in reqs]
     assert all(b > a for a, b in zip(t, t[1:]))
     assert {(r.camera.width, r.camera.height) for r in reqs} <= set(scenes.RESOLUTIONS)
+
+
+def test_training_view_cameras_pack_as_the_c_abi_reads_them():
+    """gsr_train_forward_views / gsr_train_backward_views read host arrays
+    cam_pos [V,3], cam_rot [V,9] (row-major, as cameras.json) and cam_intr
+    [V,4] = (focal_x, focal_y, z_far, z_near), view after view."""
+    import math
+
+    from polysplat_gb300.diff import _views_cam_args
+    from polysplat_gb300.rasterizer import Camera
+
+    cams = [Camera.from_spec(scenes.orbit_camera(10.0, 2 * math.pi * k / 3, 0.1 * k, 320, 180, 200.0 + k, id=k))
+            for k in range(3)]
+    pos, rot, intr = _views_cam_args(cams)
+    assert (len(pos), len(rot), len(intr)) == (9, 27, 12)
+    for v, c in enumerate(cams):
+        assert np.allclose(np.array(pos[3 * v:3 * v + 3]), c.position.numpy().reshape(-1))
+        assert np.allclose(np.array(rot[9 * v:9 * v + 9]), c.rotation.numpy().reshape(-1))
+        assert np.allclose(np.array(intr[4 * v:4 * v + 4]), [c.focal_x, c.focal_y, c.zFar, c.zNear])
