@@ -897,8 +897,9 @@ def run_diff(args, dev, rank, world, dist):
     a radius-10 orbit, L2 loss against renders of perturbed means and SH DC.
     A step is the forward of the 8 views, the loss and the backward to every
     raw parameter; `value` is views per second through `render_views` (all
-    views in one pass), and `per_view_passes` the same step with one
-    forward and backward per camera."""
+    views in one pass, quad keys), `one_pass_per_tile_keys` the same with
+    per-tile keys, and `per_view_passes` the same step with one forward and
+    backward per camera."""
     import numpy as np
     import torch
 
@@ -918,10 +919,10 @@ def run_diff(args, dev, rank, world, dist):
     for p in params:
         p.requires_grad_(True)
 
-    def step(multi=True):
+    def step(multi=True, quad=True):
         for p in params:
             p.grad = None
-        imgs = render_views(*params, cams) if multi else [render(*params, c) for c in cams]
+        imgs = render_views(*params, cams, quad_keys=quad) if multi else [render(*params, c) for c in cams]
         loss = sum(((img - tg) ** 2).sum() for img, tg in zip(imgs, targets))
         loss.backward()
         return loss
@@ -940,9 +941,9 @@ def run_diff(args, dev, rank, world, dist):
             torch.cuda.nvtx.range_end(rid)
         return {"workload": "diff_1m_8cam (profiling run)", "ranges": ["timed_views", "timed_loop"]}
 
-    def timed(multi, sampler=None):
+    def timed(multi, sampler=None, quad=True):
         for _ in range(max(3, args.warmup)):
-            step(multi)
+            step(multi, quad)
         torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()
@@ -951,7 +952,7 @@ def run_diff(args, dev, rank, world, dist):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
         for _ in range(K):
-            step(multi)
+            step(multi, quad)
         b.record()
         torch.cuda.synchronize()
         return a.elapsed_time(b) / K
@@ -960,16 +961,18 @@ def run_diff(args, dev, rank, world, dist):
     ms = timed(True, sampler)
     clocks = sampler.stop()
     ms_loop = timed(False)
+    ms_tile = timed(True, quad=False)
     ms = max_over_ranks(ms, dist, dev)
     ms_loop = max_over_ranks(ms_loop, dist, dev)
+    ms_tile = max_over_ranks(ms_tile, dist, dev)
     if rank != 0:
         return None
     views = world * len(cams) * 1000.0 / ms
     # library kernels per step: scene transform, preprocess and large-Gaussian
     # emission, sort upsweep and digit passes, tile ranges, render, render
     # backward, one adjoint per 16 views
-    tiles = ((1280 + 15) // 16) * ((720 + 15) // 16) * len(cams)
-    sort_passes = (32 + int(tiles).bit_length() + 7) // 8
+    quads = ((1280 // 16 + 1) // 2) * (((720 + 15) // 16 + 1) // 2) * len(cams)
+    sort_passes = (32 + int(quads).bit_length() + 7) // 8
     launches = 1 + 2 + 1 + sort_passes + 1 + 1 + 1 + (len(cams) + 15) // 16
     return {"metric": "views/s (forward + backward)", "value": views, "unit": "views/s", "n_gpus": world,
             "steps": K, "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
@@ -979,6 +982,8 @@ def run_diff(args, dev, rank, world, dist):
                        "l2": "scene 1 M Gaussians (0.3 GB fp32 parameters + per-view lists), larger than L2"},
             "per_view_passes": {"value": world * len(cams) * 1000.0 / ms_loop, "unit": "views/s",
                                 "ms_per_step": ms_loop},
+            "one_pass_per_tile_keys": {"value": world * len(cams) * 1000.0 / ms_tile, "unit": "views/s",
+                                       "ms_per_step": ms_tile},
             "e2e": {"value": views, "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 4},
             "gpu_launches": K * launches, "clocks": clocks}
 

@@ -389,7 +389,11 @@ gsr_status gsr_train_backward(int P, const float* means, const float* log_scales
  * (16-byte aligned) holds one record per feature row: the gradients of
  * conic/opacity (4), xy (2) and colour (3), and 3 unused.  view_scratch is
  * device memory of gsr_train_views_scratch_bytes(n_views) for the views'
- * parameter blocks; it must stay untouched until the forward has run. */
+ * parameter blocks; it must stay untouched until the forward has run.
+ * flags = GSR_QUAD_KEYS (both calls alike) sorts one key per 2x2 group of
+ * tiles (n_views * P below 2^28): ranges then hold one entry per quad
+ * (view * quads + quad), n_tile counts each tile's list positions up to its
+ * last blended Gaussian, and the images are those of per-tile keys. */
 size_t gsr_train_views_scratch_bytes(int n_views);
 gsr_status gsr_train_forward_views(int P, const float* means, const float* log_scales, const float* quats,
                                    const float* logits, const float* shs, int n_views, int width, int height,
@@ -399,7 +403,7 @@ gsr_status gsr_train_forward_views(int P, const float* means, const float* log_s
                                    size_t workspace_bytes, uint64_t* keys_unsorted, uint32_t* values_unsorted,
                                    uint64_t* keys_sorted, uint32_t* values_sorted, int64_t key_capacity,
                                    float* points_xy, float* rgb_depth, float* conic_opacity, int32_t* ranges,
-                                   int32_t* n_tile, float* T_final, float* image, gsr_stream_t stream);
+                                   int32_t* n_tile, float* T_final, float* image, int flags, gsr_stream_t stream);
 gsr_status gsr_train_backward_views(int P, const float* means, const float* log_scales, const float* quats,
                                     const float* logits, const float* shs, int n_views, int width, int height,
                                     const float* cam_pos, const float* cam_rot, const float* cam_intr,
@@ -408,7 +412,7 @@ gsr_status gsr_train_backward_views(int P, const float* means, const float* log_
                                     const float* T_final, const float* points_xy, const float* rgb_depth,
                                     const float* conic_opacity, const float* grad_image, float* grad_feat,
                                     float* g_means, float* g_log_scales, float* g_quats, float* g_logits,
-                                    float* g_shs, int accumulate, gsr_stream_t stream);
+                                    float* g_shs, int accumulate, int flags, gsr_stream_t stream);
 
 /* ---- stage timing ------------------------------------------------------- */
 /* Profiling hook with no counterpart in the reference.  After

@@ -78,9 +78,9 @@ def _declare(L):
                                   P, P, P, P, P, P, P, P, P, P, P, P, i32, P], i32)
     sig["gsr_train_views_scratch_bytes"] = ([i32], sz)
     sig["gsr_train_forward_views"] = ([i32, P, P, P, P, P, i32, i32, i32, P, P, P, P, P, P, P, sz, P, P, sz,
-                                       P, P, P, P, i64, P, P, P, P, P, P, P, P], i32)
+                                       P, P, P, P, i64, P, P, P, P, P, P, P, i32, P], i32)
     sig["gsr_train_backward_views"] = ([i32, P, P, P, P, P, i32, i32, i32, P, P, P, P, P, i64, P, P, P, P,
-                                        P, P, P, P, P, P, P, P, P, P, i32, P], i32)
+                                        P, P, P, P, P, P, P, P, P, P, i32, i32, P], i32)
     sig["gsr_depth_first_scratch_size"] = ([i32], sz)
     sig["gsr_forward_depth_first"] = ([i32, i32, P, P, i32, P, P, i32, i32, i32, i32, P, P, f32, f32, f32, f32,
                                        P, P, sz, P, sz, P, P, P, P, i64, P, P, P, P, P, P, P], i32)

@@ -309,20 +309,23 @@ gsr_status gsr_train_forward_views(int P, const float* means, const float* log_s
                                    size_t workspace_bytes, uint64_t* keys_unsorted, uint32_t* values_unsorted,
                                    uint64_t* keys_sorted, uint32_t* values_sorted, int64_t key_capacity,
                                    float* points_xy, float* rgb_depth, float* conic_opacity, int32_t* ranges,
-                                   int32_t* n_tile, float* T_final, float* image, gsr_stream_t stream)
+                                   int32_t* n_tile, float* T_final, float* image, int flags, gsr_stream_t stream)
 {
     cudaStream_t s = (cudaStream_t)stream;
     if (P < 0 || n_views <= 0 || width <= 0 || height <= 0 || !cam_pos || !cam_rot || !cam_intr || !bg_color ||
         !curr_offset || !workspace || !ranges || !n_tile || !T_final || !image || !opacity || !cov3d ||
-        !view_scratch)
+        !view_scratch || (flags & ~GSR_QUAD_KEYS) != 0)
         return GSR_INVALID_ARG;
+    const bool quad = (flags & GSR_QUAD_KEYS) != 0;
+    if (quad && (long long)P * n_views > (long long)kQuadGidMask + 1) return GSR_INVALID_ARG;
     if (P > 0 && (!means || !log_scales || !quats || !logits || !shs || !points_xy || !rgb_depth || !conic_opacity))
         return GSR_INVALID_ARG;
     if (view_scratch_bytes < gsr_train_views_scratch_bytes(n_views)) return GSR_INVALID_ARG;
     if (workspace_bytes < sort_workspace_bytes(key_capacity) || key_capacity >= (1LL << 30)) return GSR_INVALID_ARG;
     const int tiles = div_up(width, 16) * div_up(height, 16);
-    // values carry view * P + Gaussian; tile ids view * tiles + tile
+    // values carry view * P + Gaussian; key tile ids view * kt + tile (or quad)
     if ((long long)P * n_views >= (1LL << 31) || (long long)tiles * n_views >= (1LL << 30)) return GSR_INVALID_ARG;
+    const int kt = quad ? quad_cols(div_up(width, 16)) * quad_cols(div_up(height, 16)) : tiles;
     cudaError_t e = launch_scene_prepare(P, log_scales, quats, logits, opacity, cov3d, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(workspace, 0, sizeof(uint32_t), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(curr_offset, 0, sizeof(int32_t), s);
@@ -342,12 +345,13 @@ gsr_status gsr_train_forward_views(int P, const float* means, const float* log_s
         if (st != GSR_OK) return st;
         if (hp[v].mq.capacity <= 0) return GSR_INVALID_ARG;
         hp[v].gid_base = (int)r;
-        hp[v].tile_base = v * tiles;
+        hp[v].tile_base = v * kt;
         hp[v].views = d_params;
+        hp[v].quad = quad ? 1 : 0;
     }
     if (P == 0) {
         // no Gaussian: no key, and every pixel is the background
-        e = cudaMemsetAsync(ranges, 0, sizeof(int32_t) * 2 * (size_t)tiles * n_views, s);
+        e = cudaMemsetAsync(ranges, 0, sizeof(int32_t) * 2 * (size_t)kt * n_views, s);
     } else {
         PreprocessParams base = hp[0];
         base.n_views = n_views;
@@ -360,7 +364,7 @@ gsr_status gsr_train_forward_views(int P, const float* means, const float* log_s
         sa.num = 0;
         sa.d_num = curr_offset;
         sa.cap = key_capacity;
-        sa.end_bit = 32 + bits_for((uint32_t)(tiles * n_views));
+        sa.end_bit = 32 + bits_for((uint32_t)(kt * n_views));
         sa.compress_depth = true;
         sa.keys_in = keys_unsorted;
         sa.vals_in = values_unsorted;
@@ -369,7 +373,7 @@ gsr_status gsr_train_forward_views(int P, const float* means, const float* log_s
         sa.ws = workspace;
         sa.ws_bytes = workspace_bytes;
         if ((e = launch_sort(sa, s)) != cudaSuccess) return GSR_CUDA_ERROR;
-        e = launch_tile_ranges(0, curr_offset, key_capacity, tiles * n_views, keys_sorted, ranges, false, s);
+        e = launch_tile_ranges(0, curr_offset, key_capacity, kt * n_views, keys_sorted, ranges, false, s);
     }
     if (e != cudaSuccess) return GSR_CUDA_ERROR;
     TrainRenderArgs ra = {};
@@ -377,6 +381,7 @@ gsr_status gsr_train_forward_views(int P, const float* means, const float* log_s
     ra.H = height;
     ra.P = P * n_views;
     ra.n_views = n_views;
+    ra.quad = quad ? 1 : 0;
     ra.d_num = curr_offset;
     ra.cap = key_capacity;
     ra.vals = values_sorted;
@@ -400,12 +405,14 @@ gsr_status gsr_train_backward_views(int P, const float* means, const float* log_
                                     const float* T_final, const float* points_xy, const float* rgb_depth,
                                     const float* conic_opacity, const float* grad_image, float* grad_feat,
                                     float* g_means, float* g_log_scales, float* g_quats, float* g_logits,
-                                    float* g_shs, int accumulate, gsr_stream_t stream)
+                                    float* g_shs, int accumulate, int flags, gsr_stream_t stream)
 {
     cudaStream_t s = (cudaStream_t)stream;
     if (P < 0 || n_views <= 0 || width <= 0 || height <= 0 || !cam_pos || !cam_rot || !cam_intr || !bg_color ||
-        !curr_offset || !ranges || !n_tile || !T_final || !grad_image || !grad_feat)
+        !curr_offset || !ranges || !n_tile || !T_final || !grad_image || !grad_feat || (flags & ~GSR_QUAD_KEYS) != 0)
         return GSR_INVALID_ARG;
+    const bool quad = (flags & GSR_QUAD_KEYS) != 0;
+    if (quad && (long long)P * n_views > (long long)kQuadGidMask + 1) return GSR_INVALID_ARG;
     if ((reinterpret_cast<uintptr_t>(grad_feat) & 15u) != 0) return GSR_INVALID_ARG;  // 16-byte atomics
     const int tiles = div_up(width, 16) * div_up(height, 16);
     if ((long long)P * n_views >= (1LL << 31) || (long long)tiles * n_views >= (1LL << 30)) return GSR_INVALID_ARG;
@@ -421,6 +428,7 @@ gsr_status gsr_train_backward_views(int P, const float* means, const float* log_
     ra.H = height;
     ra.P = (int)rows;
     ra.n_views = n_views;
+    ra.quad = quad ? 1 : 0;
     ra.d_num = curr_offset;
     ra.cap = key_capacity;
     ra.vals = values_sorted;

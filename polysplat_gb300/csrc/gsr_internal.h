@@ -274,6 +274,10 @@ cudaError_t launch_render(const RenderArgs& a, cudaStream_t stream);
 struct TrainRenderArgs {
     int W, H, P;
     int n_views;  // 0 or 1: one view
+    // quad keys: ranges are per 2x2 group of tiles (view * quads + quad) and
+    // values carry the hit tiles in their top bits; n_tile then counts list
+    // positions up to the last Gaussian blended, not Gaussians
+    int quad;
     const int32_t* d_num;
     long long cap;
     const uint32_t* vals;

@@ -581,7 +581,33 @@ struct TrainBatch {
     float4 con[32];
     float4 rgb[32];
     uint32_t gid[32];
+    uint32_t use[32];  // the entry belongs to this tile (quad keys: its bit is set)
 };
+
+// Where tile (tx, ty) of `view` finds its list: its own range, or with quad
+// keys its quad's range, whose entries carry the bit `qbit` when they
+// belong to this tile.
+__device__ __forceinline__ int train_list(const TrainRenderArgs& a, int view, int tile, int tx, int ty, int gx, int gy,
+                                          uint32_t& qbit)
+{
+    qbit = 0u;
+    if (!a.quad) return tile;
+    const int qgx = quad_cols(gx), qpv = qgx * quad_cols(gy);
+    qbit = 1u << (kQuadShift + ((tx & 1) | ((ty & 1) << 1)));
+    return view * qpv + (ty >> 1) * qgx + (tx >> 1);
+}
+
+// One list entry: false when it is another tile's (quad keys), else its
+// Gaussian in g.
+__device__ __forceinline__ bool train_entry(const TrainRenderArgs& a, uint32_t v, uint32_t qbit, uint32_t& g)
+{
+    if (!a.quad) {
+        g = v;
+        return true;
+    }
+    g = v & kQuadGidMask;
+    return (v & qbit) != 0u;
+}
 
 __global__ __launch_bounds__(kTrainWarps * 32) void k_render_train(const TrainRenderArgs a)
 {
@@ -590,15 +616,17 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_train(const TrainRe
     const int warp = threadIdx.x >> 5;
     TrainBatch& B = sb[warp];
     // tile: global over the views; lt: within its view
-    const int gx = (a.W + 15) / 16, tiles = gx * ((a.H + 15) / 16);
+    const int gx = (a.W + 15) / 16, gy = (a.H + 15) / 16, tiles = gx * gy;
     const int tile = blockIdx.x * kTrainWarps + warp;
     if (tile >= tiles * max(a.n_views, 1)) return;
     const int view = tile / tiles, lt = tile - view * tiles;
     const size_t pix0 = (size_t)view * a.W * a.H;
     const int n = (int)max(0LL, min((long long)*a.d_num, a.cap));
-    const int ox = (lt % gx) * 16, oy = (lt / gx) * 16;
+    const int tx = lt % gx, ty = lt / gx;
+    const int ox = tx * 16, oy = ty * 16;
     const int cb = (int)(lane & 7u) * 2, rb = (int)(lane >> 3) * 4;
-    const int2 rg = __ldg(a.ranges + tile);
+    uint32_t qbit;
+    const int2 rg = __ldg(a.ranges + train_list(a, view, tile, tx, ty, gx, gy, qbit));
     const int start = min(max(rg.x, 0), n), end = min(max(rg.y, start), n);
     float T[4][2], C[4][2][3];
 #pragma unroll
@@ -608,18 +636,22 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_train(const TrainRe
             T[i][j] = 1.0f;
             C[i][j][0] = C[i][j][1] = C[i][j][2] = 0.0f;
         }
-    int processed = 0;
+    // processed: Gaussians blended (the exit cadence counts these); used:
+    // list positions up to the last one blended, what the backward replays
+    int processed = 0, used = 0;
     bool exit_now = false;
     for (int pos = start; pos < end && !exit_now; pos += 32) {
         const int cnt = min(32, end - pos);
         __syncwarp();
         if ((int)lane < cnt) {
-            const uint32_t g = __ldg(a.vals + pos + lane);
-            if (g < (uint32_t)a.P) {
+            uint32_t g;
+            const bool mine = train_entry(a, __ldg(a.vals + pos + lane), qbit, g);
+            B.use[lane] = mine ? 1u : 0u;
+            if (mine && g < (uint32_t)a.P) {
                 B.xy[lane] = __ldg(a.xy + g);
                 B.con[lane] = __ldg(a.con + g);
                 B.rgb[lane] = __ldg(a.rgbd + g);
-            } else {  // outside the feature arrays: a transparent stand-in
+            } else {  // another tile's, or outside the feature arrays: a transparent stand-in
                 B.xy[lane] = make_float2(0.f, 0.f);
                 B.con[lane] = make_float4(0.f, 0.f, 0.f, -1e30f);
                 B.rgb[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -627,9 +659,11 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_train(const TrainRe
         }
         __syncwarp();
         for (int k = 0; k < cnt; k++) {
+            if (!B.use[k]) continue;
             const float4 rgb = B.rgb[k];
             shade<2, 4, 0, false>(C, T, ox, oy, cb, rb, B.xy[k], B.con[k], make_float3(rgb.x, rgb.y, rgb.z));
             ++processed;
+            used = pos - start + k + 1;
             if (processed % kTrainCadence == 0) {
                 bool sat = true;
 #pragma unroll
@@ -643,7 +677,7 @@ __global__ __launch_bounds__(kTrainWarps * 32) void k_render_train(const TrainRe
             }
         }
     }
-    if (lane == 0) a.n_tile[tile] = processed;
+    if (lane == 0) a.n_tile[tile] = used;
 #pragma unroll
     for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -708,15 +742,17 @@ __global__ __launch_bounds__(kTrainWarps * 32, 5) void k_render_backward(const T
     const unsigned lane = threadIdx.x & 31u;
     const int warp = threadIdx.x >> 5;
     TrainBatch& B = sb[warp];
-    const int gx = (a.W + 15) / 16, tiles = gx * ((a.H + 15) / 16);
+    const int gx = (a.W + 15) / 16, gy = (a.H + 15) / 16, tiles = gx * gy;
     const int tile = blockIdx.x * kTrainWarps + warp;
     if (tile >= tiles * max(a.n_views, 1)) return;
     const int view = tile / tiles, lt = tile - view * tiles;
     const size_t pix0 = (size_t)view * a.W * a.H;
     const int n = (int)max(0LL, min((long long)*a.d_num, a.cap));
-    const int ox = (lt % gx) * 16, oy = (lt / gx) * 16;
+    const int tx = lt % gx, ty = lt / gx;
+    const int ox = tx * 16, oy = ty * 16;
     const int cb = (int)(lane & 7u) * 2, rb = (int)(lane >> 3) * 4;
-    const int2 rg = __ldg(a.ranges + tile);
+    uint32_t qbit;
+    const int2 rg = __ldg(a.ranges + train_list(a, view, tile, tx, ty, gx, gy, qbit));
     const int start = min(max(rg.x, 0), n);
     const int count = min(max(__ldg(a.n_tile + tile), 0), max(0, min(max(rg.y, start), n) - start));
     float T[4][2], R[4][2][3], G[4][2][3];
@@ -740,8 +776,10 @@ __global__ __launch_bounds__(kTrainWarps * 32, 5) void k_render_backward(const T
         const int lo = max(start, hi - 32), cnt = hi - lo;
         __syncwarp();
         if ((int)lane < cnt) {
-            const uint32_t g = __ldg(a.vals + lo + lane);
-            const bool ok = g < (uint32_t)a.P;
+            uint32_t g;
+            const bool mine = train_entry(a, __ldg(a.vals + lo + lane), qbit, g);
+            const bool ok = mine && g < (uint32_t)a.P;
+            B.use[lane] = mine ? 1u : 0u;
             B.gid[lane] = ok ? g : 0xFFFFFFFFu;
             B.xy[lane] = ok ? __ldg(a.xy + g) : make_float2(0.f, 0.f);
             B.con[lane] = ok ? __ldg(a.con + g) : make_float4(0.f, 0.f, 0.f, -1e30f);
@@ -749,6 +787,7 @@ __global__ __launch_bounds__(kTrainWarps * 32, 5) void k_render_backward(const T
         }
         __syncwarp();
         for (int k = cnt - 1; k >= 0; k--) {
+            if (!B.use[k]) continue;  // another tile of the quad
             const float2 xy = B.xy[k];
             const float4 co = B.con[k];
             const float4 c4 = B.rgb[k];

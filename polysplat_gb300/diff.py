@@ -127,9 +127,10 @@ class _RenderViewsFn(torch.autograd.Function):
     """All views in one pass (gsr_train_forward_views / gsr_train_backward_views)."""
 
     @staticmethod
-    def forward(ctx, means, log_scales, quats, logits, shs, cams, bg, key_capacity):
+    def forward(ctx, means, log_scales, quats, logits, shs, cams, bg, key_capacity, quad_keys=True):
         dev = means.device
         P, V = means.shape[0], len(cams)
+        flags = R.QUAD_KEYS if quad_keys else 0
         W, H = cams[0].width, cams[0].height
         tiles = ((W + 15) // 16) * ((H + 15) // 16)
         pos, rot, intr = _views_cam_args(cams)
@@ -153,7 +154,7 @@ class _RenderViewsFn(torch.autograd.Function):
                 P, *[_p(t) for t in params], V, W, H, pos, rot, intr, bgc, _p(b["opacity"]), _p(b["cov3d"]),
                 _p(scratch), scratch.numel(), _p(b["count"]), _p(b["ws"]), b["ws"].numel(), _p(b["ku"]), _p(b["vu"]),
                 _p(b["ks"]), _p(b["vs"]), cap, _p(b["xy"]), _p(b["rgbd"]), _p(b["con"]), _p(b["ranges"]),
-                _p(b["n_tile"]), _p(b["T"]), _p(b["image"]), stream), "train_forward_views")
+                _p(b["n_tile"]), _p(b["T"]), _p(b["image"]), flags, stream), "train_forward_views")
             n = ctypes.c_int32(0)
             st = lib().gsr_read_status(_p(b["ws"]), _p(b["count"]), cap, ctypes.byref(n), stream)
             if st == R.GSR_OVERFLOW:
@@ -165,7 +166,7 @@ class _RenderViewsFn(torch.autograd.Function):
             break
         for k in ("ku", "ks", "ws", "opacity", "cov3d"):
             del b[k]
-        ctx.b, ctx.cams, ctx.bg, ctx.cap = b, list(cams), [float(v) for v in bg], cap
+        ctx.b, ctx.cams, ctx.bg, ctx.cap, ctx.flags = b, list(cams), [float(v) for v in bg], cap, flags
         ctx.save_for_backward(*params)
         ctx.num_rendered = n.value
         return b["image"]
@@ -185,27 +186,31 @@ class _RenderViewsFn(torch.autograd.Function):
         check(lib().gsr_train_backward_views(
             P, _p(means), _p(log_scales), _p(quats), _p(logits), _p(shs), V, cams[0].width, cams[0].height, pos, rot,
             intr, bgc, _p(b["count"]), ctx.cap, _p(b["vs"]), _p(b["ranges"]), _p(b["n_tile"]), _p(b["T"]),
-            _p(b["xy"]), _p(b["rgbd"]), _p(b["con"]), _p(g), _p(gfeat), *[_p(t) for t in outs], 0,
+            _p(b["xy"]), _p(b["rgbd"]), _p(b["con"]), _p(g), _p(gfeat), *[_p(t) for t in outs], 0, ctx.flags,
             stream), "train_backward_views")
         ctx.b = None
         gm, gls, gq, glg, gsh = outs
-        return gm, gls, gq, glg, gsh, None, None, None
+        return gm, gls, gq, glg, gsh, None, None, None, None
 
 
 def render_views(means, log_scales, quats, logits, shs, cameras: Sequence[Camera], bg=(0.0, 0.0, 0.0),
-                 key_capacity: int = 1 << 22):
+                 key_capacity: int = 1 << 22, quad_keys: bool = True):
     """One differentiable image per camera (gradients sum over views).
 
     Cameras of one size go through one pass over all views: one preprocess
     launch, one sort of every view's keys, one render and one render backward
     over every view's tiles, and one adjoint that sums the views' gradients
-    per Gaussian (`key_capacity` is per view).  Cameras of different sizes
-    fall back to one pass per camera."""
+    per Gaussian (`key_capacity` is per view).  With `quad_keys` the sort
+    takes one key per 2x2 group of tiles (the same images; fewer keys and
+    tile bits).  Cameras of different sizes fall back to one pass per
+    camera."""
     cams = list(cameras)
     if not cams:
         return []
     if len(cams) == 1 or any((c.width, c.height) != (cams[0].width, cams[0].height) for c in cams):
         return [render(means, log_scales, quats, logits, shs, c, bg, key_capacity) for c in cams]
     cap = min(int(key_capacity) * len(cams), (1 << 30) - 1)
-    out = _RenderViewsFn.apply(means, log_scales, quats, logits, shs.reshape(shs.shape[0], 48), cams, list(bg), cap)
+    quad = bool(quad_keys) and means.shape[0] * len(cams) <= (1 << 28)
+    out = _RenderViewsFn.apply(means, log_scales, quats, logits, shs.reshape(shs.shape[0], 48), cams, list(bg), cap,
+                               quad)
     return list(out.unbind(0))

@@ -223,20 +223,22 @@ def _views_case(dev, n, views, W, H, seed=5):
     return params, cams
 
 
-def _grads(params, cams, weights, multi, key_capacity=1 << 22):
+def _grads(params, cams, weights, multi, key_capacity=1 << 22, quad=True):
     ps = [p.clone().requires_grad_(True) for p in params]
-    imgs = (render_views(*ps, cams, key_capacity=key_capacity) if multi
+    imgs = (render_views(*ps, cams, key_capacity=key_capacity, quad_keys=quad) if multi
             else [render(*ps, c, key_capacity=key_capacity) for c in cams])
     sum((img * w).sum() for img, w in zip(imgs, weights)).backward()
     return [img.detach() for img in imgs], [p.grad.detach() for p in ps]
 
 
+@pytest.mark.parametrize("quad", [True, False])
 @pytest.mark.parametrize("n,views,W,H", [(200_000, 8, 640, 360), (20_000, 18, 96, 64)])
-def test_render_views_matches_per_view_passes(cuda_device, n, views, W, H):
+def test_render_views_matches_per_view_passes(cuda_device, n, views, W, H, quad):
     """One pass over all views (one preprocess, sort, render and render
     backward over every view's tiles, and a per-Gaussian adjoint summed over
-    views, 16 views per launch) against one pass per view on the same scene
-    and cameras.  The key count is the sum of the views' counts exactly.
+    views, 16 views per launch), with per-tile and with quad keys, against
+    one pass per view (per-tile keys) on the same scene and cameras.  With
+    per-tile keys the key count is the sum of the views' counts exactly.
     Bar: images within 1e-5 except where equal keys blend in another order
     (at most 1e-4 of the pixels, and within 2/255); every parameter's
     gradient within a relative L2 error of 1e-4 of the per-view sum (float
@@ -245,7 +247,7 @@ def test_render_views_matches_per_view_passes(cuda_device, n, views, W, H):
     params, cams = _views_case(dev, n, views, W, H)
     gen = torch.Generator(device=dev).manual_seed(3)
     weights = [torch.rand((H, W, 3), device=dev, generator=gen) - 0.5 for _ in cams]
-    imgs_m, g_m = _grads(params, cams, weights, True)
+    imgs_m, g_m = _grads(params, cams, weights, True, quad=quad)
     imgs_s, g_s = _grads(params, cams, weights, False)
     # the per-view key counts, from the single-view function
     counts = []
@@ -253,8 +255,11 @@ def test_render_views_matches_per_view_passes(cuda_device, n, views, W, H):
         ps = [p.clone().requires_grad_(True) for p in params]
         counts.append(diff._RenderFn.apply(*ps, c, [0.0, 0.0, 0.0], 1 << 22).grad_fn.num_rendered)
     ps = [p.clone().requires_grad_(True) for p in params]
-    total = diff._RenderViewsFn.apply(*ps, cams, [0.0, 0.0, 0.0], (1 << 22) * views).grad_fn.num_rendered
-    assert total == sum(counts) > 0
+    total = diff._RenderViewsFn.apply(*ps, cams, [0.0, 0.0, 0.0], (1 << 22) * views, quad).grad_fn.num_rendered
+    if quad:
+        assert 0 < total < sum(counts)  # one key per quad a Gaussian touches
+    else:
+        assert total == sum(counts) > 0
     for a, b in zip(imgs_m, imgs_s):
         d = (a - b).abs()
         assert float(d.max()) <= 2.0 / 255.0
@@ -294,9 +299,9 @@ def test_render_views_of_mixed_sizes_runs_per_view(cuda_device):
 
 def test_training_view_entries_reject_bad_arguments(cuda_device):
     """The multi-view entries check their arguments before any launch: no
-    views, a parameter scratch smaller than gsr_train_views_scratch_bytes, and
-    a gradient record buffer off a 16-byte boundary (the record atomics
-    are 16 bytes wide) return GSR_INVALID_ARG."""
+    views, a parameter scratch smaller than gsr_train_views_scratch_bytes, a
+    gradient record buffer off a 16-byte boundary (the record atomics are 16
+    bytes wide) and unknown flag bits return GSR_INVALID_ARG."""
     import ctypes
 
     from polysplat_gb300._lib import GSR_INVALID_ARG, lib
@@ -317,15 +322,18 @@ def test_training_view_entries_reject_bad_arguments(cuda_device):
 
     def fwd(n_views, scratch_bytes):
         return L.gsr_train_forward_views(P, p, p, p, p, p, n_views, W, H, pos, rot, intr, bg, p, p, p,
-                                         scratch_bytes, p, p, ws, p, p, p, p, 1 << 10, p, p, p, p, p, p, p, stream)
+                                         scratch_bytes, p, p, ws, p, p, p, p, 1 << 10, p, p, p, p, p, p, p, 0, stream)
 
     assert fwd(0, 1 << 20) == GSR_INVALID_ARG
     assert fwd(V, L.gsr_train_views_scratch_bytes(V) - 1) == GSR_INVALID_ARG
 
     def bwd(grad_feat):
         return L.gsr_train_backward_views(P, p, p, p, p, p, V, W, H, pos, rot, intr, bg, p, 1 << 10, p, p, p, p,
-                                          p, p, p, p, grad_feat, p, p, p, p, p, 0, stream)
+                                          p, p, p, p, grad_feat, p, p, p, p, p, 0, 0, stream)
 
     assert bwd(ctypes.c_void_p(buf.data_ptr() + 4)) == GSR_INVALID_ARG
     assert bwd(None) == GSR_INVALID_ARG
+    # unknown flag bits
+    assert L.gsr_train_forward_views(P, p, p, p, p, p, V, W, H, pos, rot, intr, bg, p, p, p, 1 << 20, p, p, ws, p, p,
+                                     p, p, 1 << 10, p, p, p, p, p, p, p, 1, stream) == GSR_INVALID_ARG
     torch.cuda.synchronize()
