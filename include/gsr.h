@@ -141,8 +141,10 @@ gsr_status gsr_sort_bits(int num, const int32_t* d_num, int end_bit, void* works
  * the device).  Scratch is a library-owned static device array sized for
  * capacity <= 262144 pairs; larger capacities return GSR_INVALID_ARG.  The
  * first call on each device looks up that array's address (make it before
- * any stream capture on that device).  All calls share the array: calls that
- * overlap in time race and must be serialised by the caller. */
+ * any stream capture on that device) and keeps it for the life of the
+ * process, so it is not for use after cudaDeviceReset on that device.  All
+ * calls share the array: calls that overlap in time race and must be
+ * serialised by the caller. */
 gsr_status gsr_sort_bits_static(int num, const int32_t* d_num, int end_bit, const uint64_t* keys_in,
                                 const uint32_t* values_in, uint64_t* keys_out, uint32_t* values_out,
                                 int64_t capacity, gsr_stream_t stream);
