@@ -544,7 +544,7 @@ def run_serve_profile(args, dev):
     from polysplat_gb300.serving import Server, TuneConfig
 
     raws, reqs = scenes.serve_mix()
-    scs = [Scene.from_raw(r, dev) for r in raws]
+    scs = [Scene.from_raw(r, dev, keep_fp32_sh=False) for r in raws]
     cfg = TuneConfig(**json.loads(args.serve_profile))
     srv = Server(scs, dev, 60 << 30, cfg)
     for _ in range(2):
@@ -647,7 +647,8 @@ def run_serve(args, dev, rank, world, dist):
 
     budget = 60 << 30
     raws, reqs = scenes.serve_mix()
-    scs = [Scene.from_raw(r, dev) for r in raws]
+    # every served path reads FP16 SH: the scenes keep no FP32 copy
+    scs = [Scene.from_raw(r, dev, keep_fp32_sh=False) for r in raws]
     torch.cuda.synchronize()
     K = max(1, args.steps if args.steps is not None else 10)
     W = max(3, args.warmup)

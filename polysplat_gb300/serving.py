@@ -219,7 +219,11 @@ class Server:
     def __init__(self, scenes, device, budget_bytes: int = 60 << 30, config: Optional[TuneConfig] = None,
                  small_slots: int = 2, large_slots: int = 2, bg=(0.0, 0.0, 0.0),
                  large_capacity: Optional[int] = None):
-        """``large_capacity`` caps the key capacity of each large-lane buffer
+        """``budget_bytes`` bounds the buffer sets the server allocates; the
+        resident scenes are the caller's and are not counted.  Every lane
+        reads FP16 SH (``Scene.shs_half``), so scenes built with
+        ``keep_fp32_sh=False`` hold 136 bytes per Gaussian on the device.
+        ``large_capacity`` caps the key capacity of each large-lane buffer
         set below what the budget allows (by default the largest power of
         two up to 2^28 keys whose buffer sets fit in half the budget)."""
         self.scenes = scenes
