@@ -101,6 +101,8 @@ gsr_status preprocess_params(PreprocessParams& p, int P, const float* pos, const
     p.n_views = 0;
     p.massive_area = kDefaultMassiveArea;
     p.huge_area = kDefaultHugeArea;
+    p.quad = 0;
+    p.interleave = 0;
     p.P = P;
     p.pos = pos;
     p.shs = shs;
