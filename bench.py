@@ -5,8 +5,8 @@
 Default workload: ``serve_mix``, a stream of 512 render requests (Poisson
 arrivals at 240/s) over resident scenes of 0.5, 2, 5 and 10 M Gaussians at
 720p-2160p, served by continuous batching against the plain per-request
-forward; a step is one request, and the line also carries a config-1 plain
-forward measurement.
+forward; a step is one request, and the line also carries a plain_3m_1080p
+plain-forward measurement.
 
 Plain-forward workloads (``plain_3m_1080p``: 3,000,000 Gaussians, clustered
 with a heavy-tailed scale distribution, 1920x1080, fx=fy=1400, 16x16 tiles,
@@ -58,7 +58,7 @@ def parse():
                          "request stream (serve_mix, default 10)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", default="serve_mix",
-                    help="serve_mix (config 3, the headline), or a plain-forward workload: plain_3m_1080p, "
+                    help="serve_mix (the served stream, the headline), or a plain-forward workload: plain_3m_1080p, "
                          "plain_100k_800x600, clustered_1m_1080p, city_20m_8k; diff_1m_8cam (forward + "
                          "backward); gather_plain_3m_1080p, prepare_plain_3m (the feature gather or the scene "
                          "transform alone)")
@@ -629,7 +629,7 @@ CPU_SAMPLE_REQUESTS = 20
 
 
 def run_serve(args, dev, rank, world, dist):
-    """Config 3: resident scenes of 0.5/2/5/10 M Gaussians, 512 requests
+    """serve_mix: resident scenes of 0.5/2/5/10 M Gaussians, 512 requests
     arriving by a Poisson process at 240/s, resolutions 720p-2160p, 60 GB
     admission budget.  A step is one saturated pass over the whole stream
     (all 512 requests queued at once), served through Server.run with every
@@ -732,7 +732,7 @@ def run_serve(args, dev, rank, world, dist):
     gc.collect()
     torch.cuda.empty_cache()
 
-    # the plain forward of config 1 on the same GPU: stage times and the
+    # the plain forward of plain_3m_1080p on the same GPU: stage times and the
     # roofline of its dominant kernel
     fargs = argparse.Namespace(**vars(args))
     fargs.workload, fargs.steps, fargs.quick, fargs.no_cpu_baseline = "plain_3m_1080p", 200, False, True
@@ -758,7 +758,7 @@ def run_serve(args, dev, rank, world, dist):
             "dtype": "f32", "data": "synthetic",
             "config": serve_config(raws, reqs, world),
             "gpu_launches": launches, "clocks": clocks, "cpu_baseline": cpu,
-            "roofline": dict(fwd["roofline"], workload="plain_3m_1080p (config 1 forward)") if fwd else None,
+            "roofline": dict(fwd["roofline"], workload="plain_3m_1080p (plain forward)") if fwd else None,
             "forward": {k: fwd[k] for k in ("value", "ms_per_step", "stages_ms", "quad_keys", "e2e", "reference_gpu",
                                             "config")} if fwd else None,
             "autotune": {"candidates": len(table), "sample_requests": 128,
@@ -894,7 +894,7 @@ def run_prepare(args, dev, rank, world, dist):
 
 
 def run_diff(args, dev, rank, world, dist):
-    """Config 4: 1 M Gaussians (means ~ N(0, 3^2 I)), 8 cameras at 1280x720 on
+    """diff_1m_8cam: 1 M Gaussians (means ~ N(0, 3^2 I)), 8 cameras at 1280x720 on
     a radius-10 orbit, L2 loss against renders of perturbed means and SH DC.
     A step is the forward of the 8 views, the loss and the backward to every
     raw parameter; `value` is views per second through `render_views` (all

@@ -80,8 +80,8 @@ def test_gradients_match_fp64_finite_differences(cuda_device):
     assert good.sum() >= 60, list(zip(picks, gg, fd))
 
 
-def test_gradients_config4_distribution(cuda_device):
-    """The config-4 distribution (means ~ N(0, 3^2 I), 8 cameras on a
+def test_gradients_1m_8cam_distribution(cuda_device):
+    """The diff_1m_8cam distribution (means ~ N(0, 3^2 I), 8 cameras on a
     radius-10 orbit), subsampled to 4000 Gaussians at 256x144 so the FP64
     oracle evaluates the loss quickly; same bar as above."""
     import math
@@ -128,12 +128,12 @@ def test_gradients_config4_distribution(cuda_device):
     fd, gg = np.array(fd), np.array(gg)
     for col, name in ((0, "per view"), (1, "all views in one pass")):
         good = np.abs(gg[:, col] - fd) <= 0.05 * np.abs(fd) + 0.01 * np.abs(fd).max()
-        print("\nconfig-4 distribution, %s: agree %d/64" % (name, good.sum()))
+        print("\ndiff_1m_8cam distribution, %s: agree %d/64" % (name, good.sum()))
         assert good.sum() >= 60, name
 
 
-def test_gradients_config4_full_scene_tile_sampled(cuda_device):
-    """Config 4 at full size: 1 M Gaussians (means ~ N(0, 3^2 I)), 8 cameras
+def test_gradients_1m_8cam_full_scene_tile_sampled(cuda_device):
+    """diff_1m_8cam at full size: 1 M Gaussians (means ~ N(0, 3^2 I)), 8 cameras
     at 1280x720 on a radius-10 orbit, L2 loss against renders of the scene
     with means perturbed by N(0, 0.05^2) and SH DC by N(0, 0.1^2).  The GPU
     gradients are checked against FP64 central differences (h = 1e-4) of
@@ -166,7 +166,7 @@ def test_gradients_config4_full_scene_tile_sampled(cuda_device):
         sum(((img - tg) ** 2).sum() for img, tg in zip(imgs, targets)).backward()
         return [p.grad.detach().cpu().numpy().astype(np.float64) for p in params]
 
-    # the per-view passes and the one pass over all views (the config-4
+    # the per-view passes and the one pass over all views (the diff_1m_8cam
     # bench's path), against the same differences
     grads, grads_multi = grads_of(False), grads_of(True)
     tnp = [tg.cpu().numpy().astype(np.float64) for tg in targets]
@@ -207,7 +207,7 @@ def test_gradients_config4_full_scene_tile_sampled(cuda_device):
         misses = [(names[k], g, j, float(a), float(b))
                   for (k, g, j), a, b, ok in zip(picks, gg[:, col], fd, good) if not ok]
         rel = np.abs(gg[:, col] - fd) / (np.abs(fd) + 1e-12)
-        print("\nconfig 4, 1 M Gaussians, 8 x 1280x720, %s: agree %d/64, median rel err %.2e; misses (param, "
+        print("\ndiff_1m_8cam, 1 M Gaussians, 8 x 1280x720, %s: agree %d/64, median rel err %.2e; misses (param, "
               "gaussian, index, gpu, fp64): %s" % (path, good.sum(), float(np.median(rel)), misses))
         assert good.sum() >= 60, (path, misses)
 

@@ -173,8 +173,8 @@ def test_whole_frame_vs_reference(cuda_device, case):
 
 
 @pytest.mark.slow
-def test_config2_frame_vs_reference(cuda_device):
-    """Config 2 (20 M Gaussians, 7680x4320) end to end: the reference's own
+def test_city_20m_8k_frame_vs_reference(cuda_device):
+    """city_20m_8k (20 M Gaussians, 7680x4320) end to end: the reference's own
     forward (its preprocess, CUB sort and fused render, RK.Pipeline) against
     this library's E2E forward.
 
