@@ -920,11 +920,16 @@ def run_diff(args, dev, rank, world, dist):
     for p in params:
         p.requires_grad_(True)
 
+    tstack = torch.stack(targets)
+
     def step(multi=True, quad=True):
         for p in params:
             p.grad = None
-        imgs = render_views(*params, cams, quad_keys=quad) if multi else [render(*params, c) for c in cams]
-        loss = sum(((img - tg) ** 2).sum() for img, tg in zip(imgs, targets))
+        if multi:
+            # all views as one [views, H, W, 3] tensor: the L2 loss is one operation
+            loss = ((render_views(*params, cams, quad_keys=quad, stacked=True) - tstack) ** 2).sum()
+        else:
+            loss = sum(((render(*params, c) - tg) ** 2).sum() for c, tg in zip(cams, targets))
         loss.backward()
         return loss
 

@@ -194,7 +194,7 @@ class _RenderViewsFn(torch.autograd.Function):
 
 
 def render_views(means, log_scales, quats, logits, shs, cameras: Sequence[Camera], bg=(0.0, 0.0, 0.0),
-                 key_capacity: int = 1 << 22, quad_keys: bool = True):
+                 key_capacity: int = 1 << 22, quad_keys: bool = True, stacked: bool = False):
     """One differentiable image per camera (gradients sum over views).
 
     Cameras of one size go through one pass over all views: one preprocess
@@ -203,14 +203,20 @@ def render_views(means, log_scales, quats, logits, shs, cameras: Sequence[Camera
     per Gaussian (`key_capacity` is per view).  With `quad_keys` the sort
     takes one key per 2x2 group of tiles (the same images; fewer keys and
     tile bits).  Cameras of different sizes fall back to one pass per
-    camera."""
+    camera.  Returns a list of [H, W, 3] images, or with `stacked` (cameras
+    of one size) one [views, H, W, 3] tensor, so that a loss over all views
+    is one operation."""
     cams = list(cameras)
+    same = all((c.width, c.height) == (cams[0].width, cams[0].height) for c in cams) if cams else True
+    if stacked and not same:
+        raise ValueError("render_views(stacked=True) needs cameras of one size")
     if not cams:
-        return []
-    if len(cams) == 1 or any((c.width, c.height) != (cams[0].width, cams[0].height) for c in cams):
-        return [render(means, log_scales, quats, logits, shs, c, bg, key_capacity) for c in cams]
+        return [] if not stacked else torch.empty((0, 0, 0, 3), device=means.device)
+    if len(cams) == 1 or not same:
+        imgs = [render(means, log_scales, quats, logits, shs, c, bg, key_capacity) for c in cams]
+        return torch.stack(imgs) if stacked else imgs
     cap = min(int(key_capacity) * len(cams), (1 << 30) - 1)
     quad = bool(quad_keys) and means.shape[0] * len(cams) <= (1 << 28)
     out = _RenderViewsFn.apply(means, log_scales, quats, logits, shs.reshape(shs.shape[0], 48), cams, list(bg), cap,
                                quad)
-    return list(out.unbind(0))
+    return out if stacked else list(out.unbind(0))

@@ -337,3 +337,27 @@ def test_training_view_entries_reject_bad_arguments(cuda_device):
     assert L.gsr_train_forward_views(P, p, p, p, p, p, V, W, H, pos, rot, intr, bg, p, p, p, 1 << 20, p, p, ws, p, p,
                                      p, p, 1 << 10, p, p, p, p, p, p, p, 1, stream) == GSR_INVALID_ARG
     torch.cuda.synchronize()
+
+
+def test_render_views_stacked_equals_the_list(cuda_device):
+    """render_views(stacked=True) returns the views as one [views, H, W, 3]
+    tensor, the same images as the list form, with the same gradients."""
+    dev = cuda_device
+    params, cams = _views_case(dev, 50_000, 4, 320, 180)
+    gen = torch.Generator(device=dev).manual_seed(5)
+    w = torch.rand((4, 180, 320, 3), device=dev, generator=gen)
+    ps_a = [p.clone().requires_grad_(True) for p in params]
+    ps_b = [p.clone().requires_grad_(True) for p in params]
+    out = render_views(*ps_a, cams, stacked=True)
+    lst = render_views(*ps_b, cams)
+    assert tuple(out.shape) == (4, 180, 320, 3)
+    for a, b in zip(out.detach().unbind(0), lst):
+        d = (a - b.detach()).abs()
+        assert float(d.max()) <= 2.0 / 255.0 and int((d > 1e-5).sum()) <= 1e-4 * d.numel()
+    (out * w).sum().backward()
+    sum((img * wv).sum() for img, wv in zip(lst, w.unbind(0))).backward()
+    for a, b in zip(ps_a, ps_b):
+        assert float((a.grad - b.grad).norm() / b.grad.norm().clamp_min(1e-30)) <= 1e-4
+    odd = Camera.from_spec(scenes.orbit_camera(10.0, 1.0, 0.0, 128, 80, 90.0, id=9))
+    with pytest.raises(ValueError):
+        render_views(*params, cams + [odd], stacked=True)
