@@ -16,7 +16,10 @@ SH coefficients.
 launch over every view, one sort of all views' keys, one render and one
 render backward over every view's tiles, and one adjoint launch per 16 views
 that sums the views' gradients per Gaussian, so the parameters are read and
-their gradients written once per pass instead of once per camera.
+their gradients written once per pass instead of once per camera.  Its sort
+takes quad keys by default (one key per 2x2 group of tiles, the same images),
+and ``stacked=True`` returns the views as one [views, H, W, 3] tensor so a
+loss over all of them is one operation.
 """
 from __future__ import annotations
 
